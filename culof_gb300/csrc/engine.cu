@@ -1,0 +1,197 @@
+// Pipeline orchestration (the reference's culof::lof, pipeline.cu:131-207),
+// re-planned around a persistent context: one stream and grow-only
+// workspaces per context instead of seven cudaMallocs and a stream per call,
+// no cuBLAS, and a fused k-NN path whose n x n distances never reach HBM.
+#include <cstdlib>
+#include <sstream>
+
+#include "engine.cuh"
+#include "fast.cuh"
+
+namespace culof_gb300 {
+
+void throw_cuda(cudaError_t err, const char* file, int line, const char* expr) {
+    std::ostringstream os;
+    os << "CUDA error at " << file << ":" << line << " (" << expr << "): " << cudaGetErrorString(err);
+    throw Error(kCudaError, os.str());
+}
+
+void* DevBuf::get(size_t bytes) {
+    if (bytes == 0) bytes = 16;
+    if (bytes > cap_) {
+        release();
+        // Round up so slowly growing problem sizes do not reallocate every call.
+        size_t want = bytes + bytes / 8;
+        want = (want + 255) & ~static_cast<size_t>(255);
+        CG_CUDA(cudaMalloc(&ptr_, want));
+        cap_ = want;
+    }
+    return ptr_;
+}
+
+void DevBuf::release() {
+    if (ptr_) cudaFree(ptr_);
+    ptr_ = nullptr;
+    cap_ = 0;
+}
+
+void validate_lof_args(const void* points, int64_t n, int d, int k) {
+    if (points == nullptr) throw Error(kInvalidArgument, "points must not be null");
+    if (n < 2) throw Error(kInvalidArgument, "n_points must be >= 2");
+    if (d < 1) throw Error(kInvalidArgument, "n_dims must be >= 1");
+    if (k < 1 || static_cast<int64_t>(k) >= n) {
+        std::ostringstream os;
+        os << "k must satisfy 1 <= k <= n_points - 1 (got k=" << k << ", n_points=" << n << ")";
+        throw Error(kInvalidArgument, os.str());
+    }
+    if (n > 0x7FFFFFFFll) throw Error(kInvalidArgument, "n_points must be < 2^31");
+}
+
+void validate_contamination(double c) {
+    if (c > 0.5 || c != c) {
+        std::ostringstream os;
+        os << "contamination must be 'auto' or in (0, 0.5], got " << c;
+        throw Error(kInvalidArgument, os.str());
+    }
+}
+
+Engine::Engine(int device) : device_(device) {
+    CG_CUDA(cudaSetDevice(device_));
+    // A blocking stream (as pipeline.cu:64 creates): it orders with work on
+    // the legacy default stream, which callers' frameworks often use.
+    CG_CUDA(cudaStreamCreate(&own_stream_));
+    stream_ = own_stream_;
+}
+
+Engine::~Engine() {
+    if (own_stream_) {
+        cudaSetDevice(device_);
+        cudaStreamSynchronize(own_stream_);
+        cudaStreamDestroy(own_stream_);
+    }
+}
+
+// pipeline.cu:99-110: CULOF_TILE_ROWS overrides; otherwise a 2 GiB cap on
+// free memory less a 128 MiB margin.
+int Engine::tile_rows_for(int64_t n) {
+    if (const char* env = std::getenv("CULOF_TILE_ROWS")) {
+        const long forced = std::atol(env);
+        if (forced > 0) return static_cast<int>(forced < n ? forced : n);
+    }
+    size_t free_b = 0, total_b = 0;
+    CG_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    const size_t cap = size_t(2) << 30, margin = size_t(128) << 20;
+    const size_t usable = free_b > margin ? free_b - margin : 0;
+    return choose_tile_rows(n, usable < cap ? usable : cap);
+}
+
+bool Engine::use_fast_path(int64_t n, int d, int k) const {
+    int p = path_;
+    if (p == kPathAuto) {
+        if (const char* env = std::getenv("CULOF_GB300_PATH")) {
+            if (env[0] == 'g') p = kPathGeneral;
+            if (env[0] == 'f') p = kPathFast;
+        }
+    }
+    const bool ok = fast_path_supported(n, d, k);
+    if (p == kPathGeneral) return false;
+    if (p == kPathFast && !ok) throw Error(kInvalidArgument, "fast path requested but unsupported for this n/d/k");
+    return ok;
+}
+
+void Engine::knn_general(const float* xc, const float* norms, int64_t n, int d, int k,
+                         int32_t* nbr_idx, float* nbr_d2, float* kdist2) {
+    const int tile = tile_rows_for(n);
+    float* d_tile = tile_.as<float>(static_cast<size_t>(tile) * n);
+    for (int64_t row0 = 0; row0 < n; row0 += tile) {
+        const int rows = static_cast<int>((n - row0) < tile ? (n - row0) : tile);
+        distance_tile(xc, n, d, row0, rows, d_tile, stream_);
+        radix_select_rows(d_tile, norms, rows, row0, n, k, kSelectDistances, nbr_idx, nbr_d2, kdist2, stream_);
+    }
+}
+
+void Engine::knn(const float* d_x, int64_t n, int d, int k, bool normalize, int32_t* nbr_idx,
+                 float* nbr_d2, float* kdist2) {
+    validate_lof_args(d_x, n, d, k);
+    CG_CUDA(cudaSetDevice(device_));
+    float* xc = xc_.as<float>(static_cast<size_t>(n) * d);
+    double* partial = partial_.as<double>(center_partial_count(n, d));
+    double* mean = mean_.as<double>(d);
+    double* inv = inv_std_.as<double>(d);
+    float* norms = norms_.as<float>(n);
+    unsigned int* maxn = max_norm_.as<unsigned int>(1);
+    center(d_x, n, d, normalize, xc, partial, mean, inv, stream_);
+    squared_norms(xc, n, d, norms, maxn, stream_);
+    if (use_fast_path(n, d, k)) {
+        last_path_ = kPathFast;
+        knn_fast(xc, norms, n, d, k, nbr_idx, nbr_d2, kdist2);
+    } else {
+        last_path_ = kPathGeneral;
+        knn_general(xc, norms, n, d, k, nbr_idx, nbr_d2, kdist2);
+    }
+}
+
+void Engine::lof_device(const float* d_x, int64_t n, int d, int k, bool normalize, float* d_scores,
+                        float* d_nof) {
+    validate_lof_args(d_x, n, d, k);
+    const size_t nk = static_cast<size_t>(n) * k;
+    int32_t* idx = nbr_idx_.as<int32_t>(nk);
+    float* d2 = nbr_d2_.as<float>(nk);
+    float* kd = kdist2_.as<float>(n);
+    float* lrd = lrd_.as<float>(n);
+    knn(d_x, n, d, k, normalize, idx, d2, kd);
+    compute_lrd(idx, d2, kd, n, k, lrd, stream_);
+    compute_scores(idx, lrd, n, k, d_scores, d_nof, stream_);
+}
+
+void Engine::offset_device(const float* d_nof, int64_t n, double contamination, double* d_offset) {
+    validate_contamination(contamination);
+    void* scratch = offset_scratch_.get(offset_scratch_bytes());
+    contamination_offset(d_nof, n, plan_offset(n, contamination), scratch, d_offset, stream_);
+}
+
+void Engine::fit_predict_device(const float* d_x, int64_t n, int d, int k, bool normalize,
+                                double contamination, float* d_nof, int64_t* d_labels,
+                                double* d_offset) {
+    validate_lof_args(d_x, n, d, k);
+    validate_contamination(contamination);
+    float* scores = scores_.as<float>(n);
+    float* nof = d_nof ? d_nof : nof_.as<float>(n);
+    double* off = d_offset ? d_offset : offset_.as<double>(1);
+    lof_device(d_x, n, d, k, normalize, scores, nof);
+    offset_device(nof, n, contamination, off);
+    if (d_labels) labels_from_offset(nof, n, off, d_labels, stream_);
+}
+
+void Engine::lof_host(const float* x, int64_t n, int d, int k, bool normalize, float* scores) {
+    validate_lof_args(x, n, d, k);
+    if (scores == nullptr) throw Error(kInvalidArgument, "scores_out must not be null");
+    CG_CUDA(cudaSetDevice(device_));
+    float* dx = x_.as<float>(static_cast<size_t>(n) * d);
+    float* ds = scores_.as<float>(n);
+    CG_CUDA(cudaMemcpyAsync(dx, x, sizeof(float) * n * d, cudaMemcpyHostToDevice, stream_));
+    lof_device(dx, n, d, k, normalize, ds, nullptr);
+    CG_CUDA(cudaMemcpyAsync(scores, ds, sizeof(float) * n, cudaMemcpyDeviceToHost, stream_));
+    CG_CUDA(cudaStreamSynchronize(stream_));
+}
+
+void Engine::fit_predict_host(const float* x, int64_t n, int d, int k, bool normalize,
+                              double contamination, float* nof, int64_t* labels, double* offset) {
+    validate_lof_args(x, n, d, k);
+    validate_contamination(contamination);
+    CG_CUDA(cudaSetDevice(device_));
+    float* dx = x_.as<float>(static_cast<size_t>(n) * d);
+    float* dnof = nof_.as<float>(n);
+    int64_t* dlab = labels ? labels_.as<int64_t>(n) : nullptr;
+    double* doff = offset_.as<double>(1);
+    CG_CUDA(cudaMemcpyAsync(dx, x, sizeof(float) * n * d, cudaMemcpyHostToDevice, stream_));
+    fit_predict_device(dx, n, d, k, normalize, contamination, dnof, dlab, doff);
+    if (nof) CG_CUDA(cudaMemcpyAsync(nof, dnof, sizeof(float) * n, cudaMemcpyDeviceToHost, stream_));
+    if (labels) CG_CUDA(cudaMemcpyAsync(labels, dlab, sizeof(int64_t) * n, cudaMemcpyDeviceToHost, stream_));
+    double off_h = 0.0;
+    CG_CUDA(cudaMemcpyAsync(&off_h, doff, sizeof(double), cudaMemcpyDeviceToHost, stream_));
+    CG_CUDA(cudaStreamSynchronize(stream_));
+    if (offset) *offset = off_h;
+}
+
+}  // namespace culof_gb300

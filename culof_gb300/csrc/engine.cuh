@@ -1,0 +1,89 @@
+// The engine behind a culof_context: stream, device workspaces, pipeline.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "common.cuh"
+#include "prep.cuh"
+
+namespace culof_gb300 {
+
+// Grow-only device allocation. Replaces the reference's per-call Buffer RAII
+// objects (pipeline.cu:43-59): a context keeps its workspaces between calls.
+class DevBuf {
+public:
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf() { release(); }
+    void* get(size_t bytes);
+    template <typename T>
+    T* as(size_t count) {
+        return static_cast<T*>(get(count * sizeof(T)));
+    }
+    void release();
+    size_t capacity() const { return cap_; }
+
+private:
+    void* ptr_ = nullptr;
+    size_t cap_ = 0;
+};
+
+enum Path : int { kPathAuto = 0, kPathFast = 1, kPathGeneral = 2 };
+
+class Engine {
+public:
+    explicit Engine(int device);
+    ~Engine();
+    Engine(const Engine&) = delete;
+    Engine& operator=(const Engine&) = delete;
+
+    int device() const { return device_; }
+    cudaStream_t stream() const { return stream_; }
+    void set_stream(cudaStream_t s) { stream_ = s ? s : own_stream_; }
+    void set_path(int p) { path_ = p; }
+    int last_path() const { return last_path_; }
+
+    // Centre (+ z-score), norms and exact k-NN; outputs device, transposed.
+    void knn(const float* d_x, int64_t n, int d, int k, bool normalize, int32_t* nbr_idx,
+             float* nbr_d2, float* kdist2);
+    // Positive LOF scores (and optionally nof = -scores) on the device.
+    void lof_device(const float* d_x, int64_t n, int d, int k, bool normalize, float* d_scores,
+                    float* d_nof);
+    // LOF.fit + predict on the device; d_offset is a device double.
+    void fit_predict_device(const float* d_x, int64_t n, int d, int k, bool normalize,
+                            double contamination, float* d_nof, int64_t* d_labels, double* d_offset);
+    void offset_device(const float* d_nof, int64_t n, double contamination, double* d_offset);
+
+    // Host-pointer forms: copy in, run, copy out, synchronise.
+    void lof_host(const float* x, int64_t n, int d, int k, bool normalize, float* scores);
+    void fit_predict_host(const float* x, int64_t n, int d, int k, bool normalize,
+                          double contamination, float* nof, int64_t* labels, double* offset);
+
+private:
+    bool use_fast_path(int64_t n, int d, int k) const;
+    void knn_general(const float* xc, const float* norms, int64_t n, int d, int k, int32_t* nbr_idx,
+                     float* nbr_d2, float* kdist2);
+    void knn_fast(const float* xc, const float* norms, int64_t n, int d, int k, int32_t* nbr_idx,
+                  float* nbr_d2, float* kdist2);
+    int tile_rows_for(int64_t n);
+
+    int device_;
+    cudaStream_t own_stream_ = nullptr;
+    cudaStream_t stream_ = nullptr;
+    int path_ = kPathAuto;
+    int last_path_ = kPathAuto;
+
+    DevBuf x_, xc_, partial_, mean_, inv_std_, norms_, max_norm_;
+    DevBuf nbr_idx_, nbr_d2_, kdist2_, lrd_, scores_, nof_, labels_, offset_, offset_scratch_;
+    DevBuf tile_;
+    // fast path workspaces
+    DevBuf morton_, perm_, sort_tmp_, sort_hist_, cols_, rows_, knn_status_;
+};
+
+// Argument validation shared by every entry point (pipeline.cu:133-141).
+void validate_lof_args(const void* points, int64_t n, int d, int k);
+void validate_contamination(double c);
+
+}  // namespace culof_gb300

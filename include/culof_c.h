@@ -1,0 +1,144 @@
+/*
+ * culof_gb300 C ABI: the drop-in boundary of the exact-LOF fit_predict path.
+ *
+ * Plain C: pointers, sizes and status codes, no C++ types, no exceptions, no
+ * torch. Every entry point returns CULOF_OK (0) or an error status; the
+ * message of the calling thread's last failure is culof_last_error().
+ *
+ * Each function names the reference interface it replaces (paths within the
+ * Aminsed/cuLOF 0.2.0 source tree). Host-pointer entry points are synchronous
+ * like the reference's culof::lof; *_device entry points take device pointers
+ * and run asynchronously on the context's stream.
+ *
+ * Threads: a context must not be used by two threads at once. The entry
+ * points without a context argument use a per-thread default context.
+ */
+#ifndef CULOF_C_H
+#define CULOF_C_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define CULOF_API __attribute__((visibility("default")))
+#else
+#define CULOF_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CULOF_OK 0
+#define CULOF_ERR_INVALID_ARGUMENT 1 /* culof::lof's std::invalid_argument (pipeline.cu:133-141) */
+#define CULOF_ERR_CUDA 2             /* culof::CudaError (pipeline.cu:17-23)                     */
+#define CULOF_ERR_NO_DEVICE 3        /* CudaError("no CUDA device available") (pipeline.cu:142)  */
+#define CULOF_ERR_INTERNAL 4
+#define CULOF_ERR_KERNEL 5 /* a kernel reported an error status word (e.g. a bounded wait expired) */
+
+/* Path selection for culof_context_set_path. */
+#define CULOF_PATH_AUTO 0
+#define CULOF_PATH_FAST 1    /* fused distance + filtered select (small d, k <= 64)  */
+#define CULOF_PATH_GENERAL 2 /* exact distance tile + radix select (any d, any k)    */
+
+typedef struct culof_context culof_context;
+
+/* Version string of the API this library implements: "0.2.0"
+ * (src/culof/_version.py:8). */
+CULOF_API const char* culof_version(void);
+
+/* Message of the calling thread's last failed call ("" if none). */
+CULOF_API const char* culof_last_error(void);
+
+/* include/culof.h:28 culof::cuda_available(). 1 if a CUDA device is usable. */
+CULOF_API int culof_cuda_available(void);
+
+/* include/culof.h:31 culof::device_info(): "<name> (sm_XY, <SMs> SMs, <MiB> MiB)",
+ * written NUL-terminated into buf (truncated to cap). */
+CULOF_API int culof_device_info(char* buf, size_t cap);
+
+/* Contexts own a stream and grow-only device workspaces, replacing the
+ * reference's per-call Stream/Buffer objects (pipeline.cu:43-74, 148-168).
+ * The context binds to the device current at creation. */
+CULOF_API int culof_context_create(culof_context** out);
+CULOF_API void culof_context_destroy(culof_context* ctx);
+/* Run on a caller's cudaStream_t (NULL: the context's own stream). */
+CULOF_API int culof_context_set_stream(culof_context* ctx, void* cuda_stream);
+CULOF_API int culof_context_synchronize(culof_context* ctx);
+/* CULOF_PATH_* (default AUTO). Every path returns bit-identical results. */
+CULOF_API int culof_context_set_path(culof_context* ctx, int path);
+/* Path used by the last k-NN run of this context (CULOF_PATH_FAST/GENERAL). */
+CULOF_API int culof_context_last_path(culof_context* ctx);
+
+/* include/culof.h:46-47 culof::lof(points, n, d, k, normalize).
+ * points: host, row-major (n_points x n_dims) float32. scores_out: host,
+ * n_points floats (positive LOF). Synchronous. */
+CULOF_API int culof_lof(const float* points, int64_t n_points, int n_dims, int k, int normalize,
+              float* scores_out);
+CULOF_API int culof_context_lof(culof_context* ctx, const float* points, int64_t n_points, int n_dims, int k,
+                      int normalize, float* scores_out);
+
+/* src/culof/__init__.py:173-191 LOF(n_neighbors=k, contamination, normalize)
+ * .fit(X) followed by predict(): negative_outlier_factor_ (= -lof), offset_
+ * and the labels (-1 outlier, 1 inlier). contamination <= 0 means 'auto'
+ * (offset_ = -1.5); otherwise it must be in (0, 0.5] and offset_ equals
+ * np.percentile(nof, 100 * contamination) exactly. Host pointers; any
+ * output may be NULL. Synchronous. */
+CULOF_API int culof_fit_predict(const float* points, int64_t n_points, int n_dims, int k, int normalize,
+                      double contamination, float* nof_out, int64_t* labels_out,
+                      double* offset_out);
+CULOF_API int culof_context_fit_predict(culof_context* ctx, const float* points, int64_t n_points, int n_dims,
+                              int k, int normalize, double contamination, float* nof_out,
+                              int64_t* labels_out, double* offset_out);
+
+/* Device-resident forms of the two calls above (inputs already in HBM):
+ * every pointer is device memory; work is queued on the context stream and
+ * the call returns without synchronising. */
+CULOF_API int culof_context_lof_device(culof_context* ctx, const float* d_points, int64_t n_points, int n_dims,
+                             int k, int normalize, float* d_scores);
+CULOF_API int culof_context_fit_predict_device(culof_context* ctx, const float* d_points, int64_t n_points,
+                                     int n_dims, int k, int normalize, double contamination,
+                                     float* d_nof, int64_t* d_labels, double* d_offset);
+
+/* ---- stage entry points (the reference's internal stage API) ---------- */
+
+/* include/culof_internal.cuh:63 choose_tile_rows (pipeline.cu:33-38):
+ * clamp(budget_bytes / (4 n_points), 1, n_points). */
+CULOF_API int culof_choose_tile_rows(int64_t n_points, size_t budget_bytes);
+
+/* include/culof_internal.cuh:52-53 select_knn (knn.cu:119-241), same tile
+ * contract: d_tile holds rows x n_points Gram values x_(row_offset+r).x_c,
+ * converted in place to max(0, |x_r|^2 + |x_c|^2 - 2 x_r.x_c) with +inf on
+ * the diagonal; emits the k neighbours of each row in transposed layout
+ * (slot t of point i at [t * n_points + i]) and the k-th squared distance.
+ * Bit-exact with the reference's kernel for identical tile and norms. */
+CULOF_API int culof_select_knn_tile(void* cuda_stream, float* d_tile, const float* d_norms, int rows,
+                          int64_t row_offset, int64_t n_points, int k, int32_t* d_nbr_idx,
+                          float* d_nbr_d2, float* d_kdist2);
+
+/* The exact k-NN stage of culof::lof (pipeline.cu:162-195: centre, norms,
+ * distance tiles, select) with exact float32 direct-difference distances.
+ * d_points device (n x d); outputs device, transposed (k x n) + kdist2 (n). */
+CULOF_API int culof_context_knn_device(culof_context* ctx, const float* d_points, int64_t n_points, int n_dims,
+                             int k, int normalize, int32_t* d_nbr_idx, float* d_nbr_d2,
+                             float* d_kdist2);
+
+/* include/culof_internal.cuh:56-58 compute_lrd (lof.cu:32-46). Device pointers. */
+CULOF_API int culof_compute_lrd(void* cuda_stream, const int32_t* d_nbr_idx, const float* d_nbr_d2,
+                      const float* d_kdist2, int64_t n_points, int k, float* d_lrd);
+
+/* include/culof_internal.cuh:60-62 compute_scores (lof.cu:49-62). Device pointers. */
+CULOF_API int culof_compute_scores(void* cuda_stream, const int32_t* d_nbr_idx, const float* d_lrd,
+                         int64_t n_points, int k, float* d_scores);
+
+/* src/culof/__init__.py:179-185 offset_: np.percentile(d_nof, 100 * contamination)
+ * computed on the GPU (contamination <= 0: 'auto', -1.5). d_offset: device double. */
+CULOF_API int culof_context_contamination_offset_device(culof_context* ctx, const float* d_nof,
+                                              int64_t n_points, double contamination,
+                                              double* d_offset);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CULOF_C_H */

@@ -1,0 +1,242 @@
+"""GPU parity: the CUDA path through the C ABI against the CPU oracle.
+
+Integer/index outputs (neighbour indices, k-distance bits, labels) and every
+float output are compared BIT FOR BIT: the engine and the oracle compute the
+same float32 direct-difference distances, the same exact select and tie rule
+(knn.cu:190-224), and the same FP64 LRD/score sums (lof.cu:32-62).
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+from conftest import golden_case_arrays, rel_err
+
+import oracle
+from culof_gb300 import _culof, synthetic
+
+pytestmark = pytest.mark.gpu
+
+PATHS = [_culof.PATH_AUTO, _culof.PATH_GENERAL]
+
+
+def torch_cuda():
+    import torch
+
+    return torch
+
+
+def dev(a: np.ndarray):
+    torch = torch_cuda()
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def host(t) -> np.ndarray:
+    return t.cpu().numpy()
+
+
+@pytest.fixture
+def ctx():
+    c = _culof.Context()
+    yield c
+    c.close()
+
+
+def run_knn(ctx, X, k, normalize=False):
+    torch = torch_cuda()
+    n, d = X.shape
+    dx = dev(X)
+    idx = torch.full((k, n), -1, dtype=torch.int32, device="cuda")
+    d2 = torch.full((k, n), float("nan"), dtype=torch.float32, device="cuda")
+    kd = torch.full((n,), float("nan"), dtype=torch.float32, device="cuda")
+    ctx.knn_device(dx.data_ptr(), n, d, k, normalize, idx.data_ptr(), d2.data_ptr(), kd.data_ptr())
+    ctx.synchronize()
+    return host(idx), host(d2), host(kd)
+
+
+KNN_CASES = [
+    ("clusters", lambda: synthetic.clusters_with_outliers(4000, 8, seed=1), 20),
+    ("clusters_k1", lambda: synthetic.clusters_with_outliers(3000, 8, seed=2), 1),
+    ("lowdim", lambda: synthetic.reference_test_data(400, 3, seed=11, n_outliers=8), 20),
+    ("highdim", lambda: synthetic.reference_test_data(512, 32, seed=3, n_outliers=10), 15),
+    ("d5_k25", lambda: synthetic.reference_test_data(700, 5, seed=13, n_outliers=9), 25),
+    ("d16", lambda: synthetic.reference_test_data(3000, 16, seed=1, n_outliers=30), 10),
+    ("d64", lambda: synthetic.reference_test_data(1500, 64, seed=2, n_outliers=15), 35),
+    ("largek", lambda: synthetic.reference_test_data(600, 4, seed=5, n_outliers=12), 257),
+    ("k_n_minus_1", lambda: synthetic.reference_test_data(128, 2, seed=7, n_outliers=4), 127),
+    ("n2", lambda: np.array([[0.0, 1.0], [3.0, -1.0]], np.float32), 1),
+    ("ragged", lambda: synthetic.clusters_with_outliers(1001, 7, seed=4), 33),
+    ("dups", lambda: np.repeat(np.random.default_rng(4).standard_normal((50, 2)).astype(np.float32), 20, axis=0), 20),
+]
+
+
+@pytest.mark.parametrize("path", PATHS)
+@pytest.mark.parametrize("name,make,k", KNN_CASES, ids=[c[0] for c in KNN_CASES])
+def test_knn_bit_exact_vs_oracle(ctx, path, name, make, k):
+    X = make()
+    ctx.set_path(path)
+    idx, d2, kd = run_knn(ctx, X, k)
+    Xc, _, _ = oracle.center(X)
+    o_idx, o_d2, o_kd = oracle.knn(Xc, k)
+    np.testing.assert_array_equal(kd.view(np.uint32), o_kd.view(np.uint32))
+    np.testing.assert_array_equal(idx, o_idx)
+    np.testing.assert_array_equal(d2.view(np.uint32), o_d2.view(np.uint32))
+
+
+@pytest.mark.parametrize("path", PATHS)
+@pytest.mark.parametrize("normalize", [False, True])
+def test_scores_bit_exact_vs_oracle(ctx, path, normalize):
+    X = synthetic.clusters_with_outliers(5000, 8, seed=5)
+    X[:, 3] *= 40.0
+    ctx.set_path(path)
+    got = ctx.lof(X, 20, normalize)
+    want = oracle.lof(X, 20, normalize)
+    np.testing.assert_array_equal(got.view(np.uint32), want.view(np.uint32))
+
+
+def test_constant_feature_with_normalize(ctx):
+    rng = np.random.default_rng(6)
+    X = rng.standard_normal((500, 3)).astype(np.float32)
+    X[:, 1] = 7.0
+    got = ctx.lof(X, 20, True)
+    assert np.isfinite(got).all()
+    np.testing.assert_array_equal(got, oracle.lof(X, 20, True))
+
+
+@pytest.mark.parametrize("contamination", ["auto", 0.001, 0.01, 0.0123, 0.1, 0.5])
+def test_fit_predict_bit_exact_vs_oracle(ctx, contamination):
+    X = synthetic.clusters_with_outliers(6000, 8, seed=9)
+    nof, labels, off = ctx.fit_predict(X, 20, False, contamination)
+    o_labels, o_nof, o_off = oracle.fit_predict(X, 20, contamination)
+    np.testing.assert_array_equal(nof, o_nof)
+    assert off == o_off
+    np.testing.assert_array_equal(labels, o_labels)
+
+
+def test_offset_and_labels_match_reference_python_layer(ctx, ref_layer_golden):
+    torch = torch_cuda()
+    for case in ref_layer_golden.meta["cases"]:
+        scores = ref_layer_golden[f"{case['scores']}/scores"]
+        nof = dev(-scores)
+        off = torch.zeros(1, dtype=torch.float64, device="cuda")
+        ctx.offset_device(nof.data_ptr(), case["n"], case["contamination"], off.data_ptr())
+        ctx.synchronize()
+        assert float(off.item()) == case["offset"], case
+
+
+@pytest.mark.parametrize("rows,row_offset,k", [(40, 100, 17), (1, 0, 1), (300, 0, 299), (7, 293, 64)])
+def test_select_knn_tile_bit_exact_with_injected_distances(rows, row_offset, k):
+    """The reference's select contract (culof_internal.cuh:37-53) fed exact
+    distances: norms 0 and tile = -d2/2 make raw = d2 exactly."""
+    torch = torch_cuda()
+    rng = np.random.default_rng(rows + k)
+    n = 300
+    D = np.abs(rng.standard_normal((rows, n))).astype(np.float32) ** 3
+    D[:, ::5] = D[:, 2:3]  # exact ties at many columns
+    D[:, 7] = 0.0
+    tile_np = (-D / 2).astype(np.float32)
+    tile = dev(tile_np)
+    norms = torch.zeros(n, dtype=torch.float32, device="cuda")
+    idx = torch.full((k, n), -1, dtype=torch.int32, device="cuda")
+    d2 = torch.full((k, n), float("nan"), dtype=torch.float32, device="cuda")
+    kd = torch.full((n,), float("nan"), dtype=torch.float32, device="cuda")
+    _culof.select_knn_tile(0, tile.data_ptr(), norms.data_ptr(), rows, row_offset, n, k, idx.data_ptr(),
+                           d2.data_ptr(), kd.data_ptr())
+    torch.cuda.synchronize()
+    o_idx, o_d2, o_kd = oracle.ref_select_tile(tile_np, np.zeros(n, np.float32), row_offset, k)
+    cols = slice(row_offset, row_offset + rows)
+    np.testing.assert_array_equal(host(kd)[cols].view(np.uint32), o_kd[cols].view(np.uint32))
+    np.testing.assert_array_equal(host(idx)[:, cols], o_idx[:, cols])
+    np.testing.assert_array_equal(host(d2)[:, cols].view(np.uint32), o_d2[:, cols].view(np.uint32))
+    # the tile was converted in place to distances, diagonal +inf (knn.cu:150-152)
+    conv = host(tile)
+    expect = D.copy()
+    expect[np.arange(rows), row_offset + np.arange(rows)] = np.inf
+    np.testing.assert_array_equal(conv, expect)
+
+
+def test_select_knn_tile_on_a_gram_tile():
+    """A real Gram tile (float32 GEMM) with real norms: identical to the CPU
+    restatement of the reference's conversion and select."""
+    torch = torch_cuda()
+    X = synthetic.clusters_with_outliers(2000, 8, seed=12)
+    Xc, _, _ = oracle.center(X)
+    norms_np = oracle.norms(Xc)
+    rows, row0, k = 64, 512, 20
+    G = (Xc[row0:row0 + rows].astype(np.float64) @ Xc.T.astype(np.float64)).astype(np.float32)
+    tile = dev(G)
+    norms = dev(norms_np)
+    n = X.shape[0]
+    idx = torch.full((k, n), -1, dtype=torch.int32, device="cuda")
+    d2 = torch.full((k, n), float("nan"), dtype=torch.float32, device="cuda")
+    kd = torch.full((n,), float("nan"), dtype=torch.float32, device="cuda")
+    _culof.select_knn_tile(0, tile.data_ptr(), norms.data_ptr(), rows, row0, n, k, idx.data_ptr(), d2.data_ptr(),
+                           kd.data_ptr())
+    torch.cuda.synchronize()
+    o_idx, o_d2, o_kd = oracle.ref_select_tile(G, norms_np, row0, k)
+    cols = slice(row0, row0 + rows)
+    np.testing.assert_array_equal(host(kd)[cols].view(np.uint32), o_kd[cols].view(np.uint32))
+    np.testing.assert_array_equal(host(idx)[:, cols], o_idx[:, cols])
+
+
+def test_lrd_and_score_stage_entry_points():
+    torch = torch_cuda()
+    X = synthetic.clusters_with_outliers(3000, 8, seed=8)
+    Xc, _, _ = oracle.center(X)
+    idx, d2, kd = oracle.knn(Xc, 20)
+    n, k = X.shape[0], 20
+    lrd = torch.empty(n, dtype=torch.float32, device="cuda")
+    sc = torch.empty(n, dtype=torch.float32, device="cuda")
+    didx, dd2, dkd = dev(idx), dev(d2), dev(kd)
+    _culof.compute_lrd(0, didx.data_ptr(), dd2.data_ptr(), dkd.data_ptr(), n, k, lrd.data_ptr())
+    _culof.compute_scores(0, didx.data_ptr(), lrd.data_ptr(), n, k, sc.data_ptr())
+    torch.cuda.synchronize()
+    o_lrd = oracle.lrd(idx, d2, kd)
+    np.testing.assert_array_equal(host(lrd), o_lrd)
+    np.testing.assert_array_equal(host(sc), oracle.score(idx, o_lrd))
+
+
+def test_repeated_calls_are_bit_identical(ctx):
+    X = synthetic.reference_test_data(512, 6, seed=17, n_outliers=7)
+    first = ctx.lof(X, 20)
+    for _ in range(3):
+        np.testing.assert_array_equal(first, ctx.lof(X, 20))
+
+
+@pytest.mark.parametrize("rows", ["1", "7", "64", "699"])
+def test_tiling_does_not_change_results(monkeypatch, rows):
+    """test_culof.cu:168-183, but bit-exact: tile height changes nothing."""
+    X = synthetic.reference_test_data(700, 5, seed=13, n_outliers=9)
+    monkeypatch.delenv("CULOF_TILE_ROWS", raising=False)
+    with _culof.Context() as c:
+        c.set_path(_culof.PATH_GENERAL)
+        whole = c.lof(X, 25)
+        monkeypatch.setenv("CULOF_TILE_ROWS", rows)
+        np.testing.assert_array_equal(whole, c.lof(X, 25))
+
+
+GOLDEN = golden_case_arrays()
+
+
+@pytest.mark.parametrize("name", sorted(GOLDEN))
+def test_golden_scores_vs_sklearn(ctx, name, sk_golden):
+    """The engine against scikit-learn fixtures (test_parity.py:20-67, REL_TOL
+    2e-4), and bit-exact with the oracle."""
+    X, k, normalize = GOLDEN[name]
+    got = ctx.lof(X, k, normalize)
+    np.testing.assert_array_equal(got, oracle.lof(X, k, normalize))
+    want = sk_golden[f"{name}/scores"]
+    rel = rel_err(got, want)
+    if name == "duplicates":
+        assert np.max(np.abs(got - want)) < 1e-2
+        return
+    bad = np.flatnonzero(rel >= 2e-4)
+    if len(bad):
+        gap = (sk_golden[f"{name}/dist_k1"] - sk_golden[f"{name}/dist_k"]) / np.maximum(sk_golden[f"{name}/dist_k"],
+                                                                                           1e-12)
+        assert gap[bad].max() < 1e-3
+    if X.shape[0] >= 20_000:
+        assert np.median(rel) < 1e-6 and np.percentile(rel, 99) < 1e-5
+        nof, labels, _ = ctx.fit_predict(X, k, normalize, 0.01)
+        want_out = np.unpackbits(sk_golden[f"{name}/outlier_bits"])[: X.shape[0]].astype(bool)
+        assert np.array_equal(labels == -1, want_out)

@@ -1,0 +1,117 @@
+"""Host-side logic and the C-ABI boundary, no GPU needed.
+
+Mirrors the reference's CPU-checkable contract: argument validation and its
+messages (src/culof/__init__.py:37-80, 159-171; pipeline.cu:133-141),
+choose_tile_rows (test_culof.cu:207-212), repr/version/__all__ (test_api.py,
+test_regressions.py), and that the library loads and exports every entry
+point include/*.h declares.
+"""
+
+from __future__ import annotations
+
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+from conftest import ROOT
+
+import culof_gb300
+from culof_gb300 import LOF, _culof, lof
+
+
+def declared_c_symbols() -> list[str]:
+    text = open(os.path.join(ROOT, "include", "culof_c.h")).read()
+    return re.findall(r"CULOF_API\s+[\w\s\*]*?\b(culof_\w+)\s*\(", text)
+
+
+def test_library_exports_every_declared_c_symbol():
+    names = declared_c_symbols()
+    assert len(names) >= 20
+    for name in names:
+        assert hasattr(_culof._lib, name), name
+    assert set(names) == set(_culof.EXPORTED)
+
+
+def test_library_exports_cxx_api():
+    out = subprocess.run(["nm", "-D", "-C", "--defined-only", _culof.LIB_PATH], capture_output=True, text=True)
+    if out.returncode != 0:
+        pytest.skip("nm unavailable")
+    for sig in ("culof::lof(float const*, int, int, int, bool)", "culof::cuda_available()", "culof::device_info"):
+        assert sig in out.stdout, sig
+
+
+def test_choose_tile_rows_respects_budget():
+    # test_culof.cu:207-212: 1000 points is 4000 bytes per row
+    assert _culof.choose_tile_rows(1000, 40000) == 10
+    assert _culof.choose_tile_rows(1000, 0) == 1
+    assert _culof.choose_tile_rows(1000, 1 << 40) == 1000
+
+
+def test_version_and_surface(ref_layer_golden):
+    meta = ref_layer_golden.meta
+    assert culof_gb300.__version__ == meta["version"] == _culof.version()
+    assert sorted(culof_gb300.__all__) == sorted(meta["all"])
+    assert repr(LOF(n_neighbors=7)) == meta["repr"]
+
+
+@pytest.mark.parametrize(
+    "label,call",
+    [
+        ("k0", lambda: LOF(n_neighbors=0)),
+        ("contam_bad", lambda: LOF(contamination=0.9)),
+        ("k_too_big", lambda: LOF(n_neighbors=100).fit(np.zeros((100, 2), np.float32))),
+        ("not_2d", lambda: lof(np.zeros(10, np.float32), 3)),
+        ("nan", lambda: lof(np.array([[0.0, np.nan], [1.0, 1.0], [2.0, 2.0]], np.float32), 1)),
+        ("overflow", lambda: lof((np.ones((64, 4)) * 1e20).astype(np.float32), 5)),
+        ("no_features", lambda: lof(np.zeros((5, 0), np.float32), 1)),
+        ("unfitted", lambda: LOF().predict()),
+    ],
+)
+def test_validation_messages_match_reference(label, call, ref_layer_golden):
+    kind, msg = ref_layer_golden.meta["errors"][label]
+    with pytest.raises(ValueError) as ei:
+        call()
+    assert type(ei.value).__name__ == kind
+    assert str(ei.value) == msg
+
+
+@pytest.mark.parametrize("bad", [0.0, 0.9, 1.0, -0.1])
+def test_rejects_bad_contamination(bad):
+    with pytest.raises(ValueError, match="contamination"):
+        LOF(contamination=bad)
+
+
+def test_predict_and_score_samples_take_no_x():
+    m = LOF()
+    with pytest.raises(TypeError):
+        m.predict(np.zeros((3, 2)))
+    with pytest.raises(TypeError):
+        m.score_samples(np.zeros((3, 2)))
+
+
+def test_c_abi_argument_errors_before_device_check():
+    """Invalid arguments are reported as ValueError (std::invalid_argument in
+    the reference, checked before cuda_available, pipeline.cu:133-142)."""
+    X = np.zeros((50, 2), np.float32)
+    with pytest.raises(ValueError, match="k must satisfy"):
+        _culof.lof(X, 50, False)
+    with pytest.raises(ValueError, match="k must satisfy"):
+        _culof.lof(X, 0, False)
+    with pytest.raises(ValueError, match="n_points must be >= 2"):
+        _culof.lof(X[:1], 1, False)
+    with pytest.raises(ValueError, match="2-D"):
+        _culof.lof(X.ravel(), 1, False)
+
+
+def test_no_device_raises_cuda_error(gpu_available):
+    if gpu_available:
+        pytest.skip("a device is present")
+    assert culof_gb300.cuda_available() is False
+    assert culof_gb300.device_info() == "no CUDA device"
+    with pytest.raises(culof_gb300.CudaError, match="no CUDA device available"):
+        _culof.lof(np.random.default_rng(0).standard_normal((50, 2)).astype(np.float32), 5, False)
+    assert issubclass(culof_gb300.CudaError, RuntimeError)
+    with pytest.raises(culof_gb300.CudaError):
+        _culof.Context()
