@@ -116,7 +116,7 @@ int culof_context_set_stream(culof_context* ctx, void* cuda_stream) {
 }
 
 int culof_context_synchronize(culof_context* ctx) {
-    return guarded([&] { CG_CUDA(cudaStreamSynchronize(engine_of(ctx).stream())); });
+    return guarded([&] { engine_of(ctx).check_status(); });
 }
 
 int culof_context_set_path(culof_context* ctx, int path) {
@@ -214,7 +214,7 @@ int culof_compute_lrd(void* cuda_stream, const int32_t* d_nbr_idx, const float* 
         if (!d_nbr_idx || !d_nbr_d2 || !d_kdist2 || !d_lrd)
             throw Error(culof_gb300::kInvalidArgument, "device pointers must not be null");
         if (n_points < 1 || k < 1) throw Error(culof_gb300::kInvalidArgument, "n_points and k must be >= 1");
-        culof_gb300::compute_lrd(d_nbr_idx, d_nbr_d2, d_kdist2, n_points, k, d_lrd,
+        culof_gb300::compute_lrd(d_nbr_idx, d_nbr_d2, d_kdist2, n_points, k, d_lrd, nullptr,
                                  static_cast<cudaStream_t>(cuda_stream));
     });
 }
@@ -225,7 +225,7 @@ int culof_compute_scores(void* cuda_stream, const int32_t* d_nbr_idx, const floa
         if (!d_nbr_idx || !d_lrd || !d_scores)
             throw Error(culof_gb300::kInvalidArgument, "device pointers must not be null");
         if (n_points < 1 || k < 1) throw Error(culof_gb300::kInvalidArgument, "n_points and k must be >= 1");
-        culof_gb300::compute_scores(d_nbr_idx, d_lrd, n_points, k, d_scores, nullptr,
+        culof_gb300::compute_scores(d_nbr_idx, d_lrd, n_points, k, d_scores, nullptr, nullptr,
                                     static_cast<cudaStream_t>(cuda_stream));
     });
 }

@@ -120,6 +120,7 @@ void Engine::knn(const float* d_x, int64_t n, int d, int k, bool normalize, int3
     double* inv = inv_std_.as<double>(d);
     float* norms = norms_.as<float>(n);
     unsigned int* maxn = max_norm_.as<unsigned int>(1);
+    CG_CUDA(cudaMemsetAsync(status_ptr(), 0, sizeof(int), stream_));
     center(d_x, n, d, normalize, xc, partial, mean, inv, stream_);
     squared_norms(xc, n, d, norms, maxn, stream_);
     if (use_fast_path(n, d, k)) {
@@ -140,8 +141,8 @@ void Engine::lof_device(const float* d_x, int64_t n, int d, int k, bool normaliz
     float* kd = kdist2_.as<float>(n);
     float* lrd = lrd_.as<float>(n);
     knn(d_x, n, d, k, normalize, idx, d2, kd);
-    compute_lrd(idx, d2, kd, n, k, lrd, stream_);
-    compute_scores(idx, lrd, n, k, d_scores, d_nof, stream_);
+    compute_lrd(idx, d2, kd, n, k, lrd, status_ptr(), stream_);
+    compute_scores(idx, lrd, n, k, d_scores, d_nof, status_ptr(), stream_);
 }
 
 void Engine::offset_device(const float* d_nof, int64_t n, double contamination, double* d_offset) {
@@ -172,7 +173,15 @@ void Engine::lof_host(const float* x, int64_t n, int d, int k, bool normalize, f
     CG_CUDA(cudaMemcpyAsync(dx, x, sizeof(float) * n * d, cudaMemcpyHostToDevice, stream_));
     lof_device(dx, n, d, k, normalize, ds, nullptr);
     CG_CUDA(cudaMemcpyAsync(scores, ds, sizeof(float) * n, cudaMemcpyDeviceToHost, stream_));
+    check_status();
+}
+
+void Engine::check_status() {
+    int st = 0;
+    CG_CUDA(cudaMemcpyAsync(&st, status_ptr(), sizeof(int), cudaMemcpyDeviceToHost, stream_));
     CG_CUDA(cudaStreamSynchronize(stream_));
+    if (st == 1) throw Error(kKernelFault, "k-NN kernel: a bounded wait on a tile copy expired");
+    if (st != 0) throw Error(kKernelFault, "k-NN kernel produced an invalid neighbour index");
 }
 
 void Engine::fit_predict_host(const float* x, int64_t n, int d, int k, bool normalize,
@@ -190,7 +199,7 @@ void Engine::fit_predict_host(const float* x, int64_t n, int d, int k, bool norm
     if (labels) CG_CUDA(cudaMemcpyAsync(labels, dlab, sizeof(int64_t) * n, cudaMemcpyDeviceToHost, stream_));
     double off_h = 0.0;
     CG_CUDA(cudaMemcpyAsync(&off_h, doff, sizeof(double), cudaMemcpyDeviceToHost, stream_));
-    CG_CUDA(cudaStreamSynchronize(stream_));
+    check_status();
     if (offset) *offset = off_h;
 }
 

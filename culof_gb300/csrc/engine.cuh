@@ -79,7 +79,16 @@ private:
     DevBuf nbr_idx_, nbr_d2_, kdist2_, lrd_, scores_, nof_, labels_, offset_, offset_scratch_;
     DevBuf tile_;
     // fast path workspaces
-    DevBuf morton_, perm_, sort_tmp_, sort_hist_, cols_, rows_, knn_status_;
+    DevBuf morton_, perm_, sort_tmp_, sort_hist_, cols_, rows_;
+    // Device status word of the current call: kernels set it (a bounded wait
+    // that expired, an out-of-range neighbour index); host paths check it.
+    DevBuf status_;
+    int* status_ptr() { return status_.as<int>(1); }
+
+public:
+    // Raises kKernelFault if a kernel of the last call reported an error
+    // (synchronises the stream).
+    void check_status();
 };
 
 // Argument validation shared by every entry point (pipeline.cu:133-141).

@@ -20,26 +20,43 @@ constexpr int kBlock = 256;
 
 __global__ void lrd_kernel(const int32_t* __restrict__ nbr_idx, const float* __restrict__ nbr_d2,
                            const float* __restrict__ kdist2, int64_t n, int k,
-                           float* __restrict__ lrd) {
+                           float* __restrict__ lrd, int* status) {
     const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    if (status != nullptr && *status != 0) {
+        lrd[i] = __int_as_float(0x7fc00000);
+        return;
+    }
     double sum = 0.0;
     for (int t = 0; t < k; ++t) {
         const int64_t o = static_cast<int64_t>(t) * n + i;
         const int32_t j = nbr_idx[o];
+        if (j < 0 || j >= n) {  // never happens for a valid k-NN graph; do not read out of range
+            if (status != nullptr) atomicExch(status, 2);
+            lrd[i] = __int_as_float(0x7fc00000);
+            return;
+        }
         sum = __dadd_rn(sum, __dsqrt_rn(static_cast<double>(fmaxf(kdist2[j], nbr_d2[o]))));
     }
     lrd[i] = __double2float_rn(__ddiv_rn(1.0, __dadd_rn(__ddiv_rn(sum, static_cast<double>(k)), 1e-10)));
 }
 
 __global__ void score_kernel(const int32_t* __restrict__ nbr_idx, const float* __restrict__ lrd,
-                             int64_t n, int k, float* __restrict__ scores, float* __restrict__ nof) {
+                             int64_t n, int k, float* __restrict__ scores, float* __restrict__ nof,
+                             int* status) {
     const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const double self = static_cast<double>(lrd[i]);
     double sum = 0.0;
-    for (int t = 0; t < k; ++t)
-        sum = __dadd_rn(sum, __ddiv_rn(static_cast<double>(lrd[nbr_idx[static_cast<int64_t>(t) * n + i]]), self));
+    for (int t = 0; t < k; ++t) {
+        const int32_t j = nbr_idx[static_cast<int64_t>(t) * n + i];
+        if (j < 0 || j >= n) {
+            if (status != nullptr) atomicExch(status, 2);
+            sum = __longlong_as_double(0x7ff8000000000000ll);
+            break;
+        }
+        sum = __dadd_rn(sum, __ddiv_rn(static_cast<double>(lrd[j]), self));
+    }
     const float s = __double2float_rn(__ddiv_rn(sum, static_cast<double>(k)));
     scores[i] = s;
     if (nof != nullptr) nof[i] = -s;
@@ -179,14 +196,16 @@ int small_grid(int64_t n) {
 }  // namespace
 
 void compute_lrd(const int32_t* nbr_idx, const float* nbr_d2, const float* kdist2, int64_t n, int k,
-                 float* lrd, cudaStream_t s) {
-    lrd_kernel<<<static_cast<unsigned>(ceil_div(n, kBlock)), kBlock, 0, s>>>(nbr_idx, nbr_d2, kdist2, n, k, lrd);
+                 float* lrd, int* status, cudaStream_t s) {
+    lrd_kernel<<<static_cast<unsigned>(ceil_div(n, kBlock)), kBlock, 0, s>>>(nbr_idx, nbr_d2, kdist2, n, k, lrd,
+                                                                             status);
     CG_LAUNCH_CHECK();
 }
 
 void compute_scores(const int32_t* nbr_idx, const float* lrd, int64_t n, int k, float* scores,
-                    float* nof, cudaStream_t s) {
-    score_kernel<<<static_cast<unsigned>(ceil_div(n, kBlock)), kBlock, 0, s>>>(nbr_idx, lrd, n, k, scores, nof);
+                    float* nof, int* status, cudaStream_t s) {
+    score_kernel<<<static_cast<unsigned>(ceil_div(n, kBlock)), kBlock, 0, s>>>(nbr_idx, lrd, n, k, scores, nof,
+                                                                               status);
     CG_LAUNCH_CHECK();
 }
 

@@ -26,10 +26,12 @@ void radix_select_rows(float* tile, const float* norms, int rows, int64_t row_of
 int choose_tile_rows(int64_t n_points, size_t budget_bytes);
 
 // ---- lof.cu ----------------------------------------------------------------
+// status (may be null): the gathers return early when it is non-zero and set
+// it to 2 if a neighbour index is out of range.
 void compute_lrd(const int32_t* nbr_idx, const float* nbr_d2, const float* kdist2, int64_t n, int k,
-                 float* lrd, cudaStream_t s);
+                 float* lrd, int* status, cudaStream_t s);
 void compute_scores(const int32_t* nbr_idx, const float* lrd, int64_t n, int k, float* scores,
-                    float* nof, cudaStream_t s);
+                    float* nof, int* status, cudaStream_t s);
 
 struct OffsetPlan {
     int64_t lo;          // lower order statistic (0-based, ascending nof)

@@ -17,10 +17,11 @@ GOLDEN = os.path.join(ROOT, "tests", "golden")
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA device (runs on the GB300 box)")
-    # Build the CUDA library and the CPU oracle once per session.
-    from culof_gb300 import _build
+    # Build the CUDA library and the CPU oracle once per session (the builder
+    # is loaded by path: importing the package needs the library it builds).
+    import __graft_entry__
 
-    _build.build()
+    __graft_entry__._load_builder().build()
     import oracle
 
     oracle.build()

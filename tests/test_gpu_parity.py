@@ -67,6 +67,16 @@ KNN_CASES = [
     ("n2", lambda: np.array([[0.0, 1.0], [3.0, -1.0]], np.float32), 1),
     ("ragged", lambda: synthetic.clusters_with_outliers(1001, 7, seed=4), 33),
     ("dups", lambda: np.repeat(np.random.default_rng(4).standard_normal((50, 2)).astype(np.float32), 20, axis=0), 20),
+    # fast-path shapes: one tile, a one-row last tile, lists of 128, d = 1
+    ("n128", lambda: synthetic.clusters_with_outliers(128, 8, seed=21), 20),
+    ("n129", lambda: synthetic.clusters_with_outliers(129, 8, seed=22), 20),
+    ("k64", lambda: synthetic.clusters_with_outliers(5000, 8, seed=23), 64),
+    ("k33_d3", lambda: synthetic.clusters_with_outliers(3000, 3, seed=24), 33),
+    ("d1", lambda: synthetic.clusters_with_outliers(2000, 1, seed=25), 10),
+    # 10,000 points on 50 positions: every point has 199 exact duplicates,
+    # which drives list overflows and the exact re-run of a block
+    ("dups_heavy", lambda: np.repeat(np.random.default_rng(5).uniform(-3, 3, (50, 4)).astype(np.float32), 200,
+                                     axis=0)[np.random.default_rng(6).permutation(10_000)], 20),
 ]
 
 
@@ -81,6 +91,16 @@ def test_knn_bit_exact_vs_oracle(ctx, path, name, make, k):
     np.testing.assert_array_equal(kd.view(np.uint32), o_kd.view(np.uint32))
     np.testing.assert_array_equal(idx, o_idx)
     np.testing.assert_array_equal(d2.view(np.uint32), o_d2.view(np.uint32))
+
+
+def test_auto_selects_the_fast_path_for_small_d(ctx):
+    X = synthetic.clusters_with_outliers(3000, 8, seed=1)
+    ctx.lof(X, 20)
+    assert ctx.last_path() == _culof.PATH_FAST
+    ctx.lof(synthetic.reference_test_data(600, 4, seed=5), 257)
+    assert ctx.last_path() == _culof.PATH_GENERAL
+    ctx.lof(synthetic.reference_test_data(600, 32, seed=5), 20)
+    assert ctx.last_path() == _culof.PATH_GENERAL
 
 
 @pytest.mark.parametrize("path", PATHS)
