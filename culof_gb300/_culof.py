@@ -61,6 +61,10 @@ _SIGS = {
     "culof_context_synchronize": ([_P], _I),
     "culof_context_set_path": ([_P, _I], _I),
     "culof_context_last_path": ([_P], _I),
+    "culof_context_set_timing": ([_P, _I], _I),
+    "culof_context_stage_times": ([_P, _P, _I], _I),
+    "culof_kernel_launch_count": ([], ctypes.c_ulonglong),
+    "culof_probe_fp32_tflops": ([_I, ctypes.POINTER(_D)], _I),
     "culof_lof": ([_P, _I64, _I, _I, _I, _P], _I),
     "culof_context_lof": ([_P, _P, _I64, _I, _I, _I, _P], _I),
     "culof_fit_predict": ([_P, _I64, _I, _I, _I, _D, _P, _P, _P], _I),
@@ -138,6 +142,18 @@ def fit_predict(points, k: int, normalize: bool, contamination):
     return nof, labels, off.value
 
 
+def kernel_launch_count() -> int:
+    """Kernels this library has launched in this process."""
+    return int(_lib.culof_kernel_launch_count())
+
+
+def probe_fp32_tflops(packed: bool = True) -> float:
+    """Measured FP32 FMA throughput of the current device (TFLOP/s)."""
+    v = _D(0.0)
+    _check(_lib.culof_probe_fp32_tflops(int(bool(packed)), ctypes.byref(v)))
+    return v.value
+
+
 def choose_tile_rows(n_points: int, budget_bytes: int) -> int:
     return int(_lib.culof_choose_tile_rows(int(n_points), int(budget_bytes)))
 
@@ -196,6 +212,21 @@ class Context:
 
     def last_path(self) -> int:
         return int(_lib.culof_context_last_path(self._h))
+
+    STAGES = ("prep", "order", "seed", "sweep", "merge", "lrd_score", "offset_labels")
+
+    def set_timing(self, on: bool) -> None:
+        _check(_lib.culof_context_set_timing(self._h, int(bool(on))))
+
+    def stage_times(self) -> dict:
+        """Milliseconds per stage of the last call (CUDA events; synchronises)."""
+        buf = (ctypes.c_float * len(self.STAGES))()
+        _check(_lib.culof_context_stage_times(self._h, buf, len(self.STAGES)))
+        return {name: float(v) for name, v in zip(self.STAGES, buf) if v >= 0}
+
+    @property
+    def handle(self) -> int:
+        return self._h.value
 
     def lof(self, points, k: int, normalize: bool = False) -> np.ndarray:
         arr = _as_points(points)

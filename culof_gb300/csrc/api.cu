@@ -133,6 +133,19 @@ int culof_context_last_path(culof_context* ctx) {
     return p;
 }
 
+int culof_context_set_timing(culof_context* ctx, int on) {
+    return guarded([&] { engine_of(ctx).set_timing(on != 0); });
+}
+
+int culof_context_stage_times(culof_context* ctx, float* ms, int cap) {
+    return guarded([&] {
+        if (ms == nullptr || cap < 0) throw Error(culof_gb300::kInvalidArgument, "ms must not be null");
+        engine_of(ctx).stage_times(ms, cap);
+    });
+}
+
+unsigned long long culof_kernel_launch_count(void) { return culof_gb300::launch_count(); }
+
 int culof_lof(const float* points, int64_t n_points, int n_dims, int k, int normalize, float* scores_out) {
     return guarded([&] {
         culof_gb300::validate_lof_args(points, n_points, n_dims, k);

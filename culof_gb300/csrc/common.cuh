@@ -33,7 +33,14 @@ void throw_cuda(cudaError_t err, const char* file, int line, const char* expr);
         if (_e != cudaSuccess) ::culof_gb300::throw_cuda(_e, __FILE__, __LINE__, #expr); \
     } while (0)
 
-#define CG_LAUNCH_CHECK() CG_CUDA(cudaGetLastError())
+// Every kernel launch of the library is followed by this check, which also
+// counts the launch (culof_kernel_launch_count in the C ABI).
+void count_launch();
+#define CG_LAUNCH_CHECK()                  \
+    do {                                   \
+        ::culof_gb300::count_launch();     \
+        CG_CUDA(cudaGetLastError());       \
+    } while (0)
 
 // Selection keys: (squared-distance bits << 32) | original column index.
 // Squared distances are never negative (and never -0.0), so their IEEE bit

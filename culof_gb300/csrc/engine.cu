@@ -2,6 +2,7 @@
 // re-planned around a persistent context: one stream and grow-only
 // workspaces per context instead of seven cudaMallocs and a stream per call,
 // no cuBLAS, and a fused k-NN path whose n x n distances never reach HBM.
+#include <atomic>
 #include <cstdlib>
 #include <sstream>
 
@@ -9,6 +10,13 @@
 #include "fast.cuh"
 
 namespace culof_gb300 {
+
+namespace {
+std::atomic<unsigned long long> g_launches{0};
+}
+
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+unsigned long long launch_count() { return g_launches.load(std::memory_order_relaxed); }
 
 void throw_cuda(cudaError_t err, const char* file, int line, const char* expr) {
     std::ostringstream os;
@@ -61,9 +69,12 @@ Engine::Engine(int device) : device_(device) {
     // the legacy default stream, which callers' frameworks often use.
     CG_CUDA(cudaStreamCreate(&own_stream_));
     stream_ = own_stream_;
+    CG_CUDA(cudaMemset(status_ptr(), 0, sizeof(int)));
 }
 
 Engine::~Engine() {
+    for (auto& e : events_)
+        if (e) cudaEventDestroy(e);
     if (own_stream_) {
         cudaSetDevice(device_);
         cudaStreamSynchronize(own_stream_);
@@ -121,15 +132,23 @@ void Engine::knn(const float* d_x, int64_t n, int d, int k, bool normalize, int3
     float* norms = norms_.as<float>(n);
     unsigned int* maxn = max_norm_.as<unsigned int>(1);
     CG_CUDA(cudaMemsetAsync(status_ptr(), 0, sizeof(int), stream_));
+    for (bool& m : marked_) m = false;
+    mark(0);
     center(d_x, n, d, normalize, xc, partial, mean, inv, stream_);
     squared_norms(xc, n, d, norms, maxn, stream_);
     if (use_fast_path(n, d, k)) {
         last_path_ = kPathFast;
+        mark(1);
         knn_fast(xc, norms, n, d, k, nbr_idx, nbr_d2, kdist2);
     } else {
         last_path_ = kPathGeneral;
+        mark(1);
+        mark(2);
+        mark(3);
         knn_general(xc, norms, n, d, k, nbr_idx, nbr_d2, kdist2);
+        mark(4);
     }
+    mark(5);
 }
 
 void Engine::lof_device(const float* d_x, int64_t n, int d, int k, bool normalize, float* d_scores,
@@ -143,6 +162,7 @@ void Engine::lof_device(const float* d_x, int64_t n, int d, int k, bool normaliz
     knn(d_x, n, d, k, normalize, idx, d2, kd);
     compute_lrd(idx, d2, kd, n, k, lrd, status_ptr(), stream_);
     compute_scores(idx, lrd, n, k, d_scores, d_nof, status_ptr(), stream_);
+    mark(6);
 }
 
 void Engine::offset_device(const float* d_nof, int64_t n, double contamination, double* d_offset) {
@@ -162,6 +182,7 @@ void Engine::fit_predict_device(const float* d_x, int64_t n, int d, int k, bool 
     lof_device(d_x, n, d, k, normalize, scores, nof);
     offset_device(nof, n, contamination, off);
     if (d_labels) labels_from_offset(nof, n, off, d_labels, stream_);
+    mark(7);
 }
 
 void Engine::lof_host(const float* x, int64_t n, int d, int k, bool normalize, float* scores) {
@@ -174,6 +195,28 @@ void Engine::lof_host(const float* x, int64_t n, int d, int k, bool normalize, f
     lof_device(dx, n, d, k, normalize, ds, nullptr);
     CG_CUDA(cudaMemcpyAsync(scores, ds, sizeof(float) * n, cudaMemcpyDeviceToHost, stream_));
     check_status();
+}
+
+void Engine::set_timing(bool on) {
+    if (on && !events_[0]) {
+        CG_CUDA(cudaSetDevice(device_));
+        for (auto& e : events_) CG_CUDA(cudaEventCreate(&e));
+    }
+    timing_ = on;
+}
+
+void Engine::mark(int boundary) {
+    if (!timing_) return;
+    CG_CUDA(cudaEventRecord(events_[boundary], stream_));
+    marked_[boundary] = true;
+}
+
+void Engine::stage_times(float* ms, int cap) {
+    CG_CUDA(cudaStreamSynchronize(stream_));
+    for (int i = 0; i < kNumStages && i < cap; ++i) {
+        ms[i] = -1.0f;
+        if (timing_ && marked_[i] && marked_[i + 1]) CG_CUDA(cudaEventElapsedTime(&ms[i], events_[i], events_[i + 1]));
+    }
 }
 
 void Engine::check_status() {

@@ -89,7 +89,24 @@ public:
     // Raises kKernelFault if a kernel of the last call reported an error
     // (synchronises the stream).
     void check_status();
+
+    // Stage timing with CUDA events on the launching stream. Stages:
+    // 0 centre+norms, 1 spatial order+tiles, 2 seed, 3 sweep (or the general
+    // path's tile+select), 4 merge, 5 lrd+score, 6 offset+labels.
+    static constexpr int kNumStages = 7;
+    void set_timing(bool on);
+    // Milliseconds per stage of the last call (synchronises); -1 if a stage
+    // did not run.
+    void stage_times(float* ms, int cap);
+    void mark(int boundary);
+
+private:
+    bool timing_ = false;
+    cudaEvent_t events_[kNumStages + 1] = {};
+    bool marked_[kNumStages + 1] = {};
 };
+
+unsigned long long launch_count();
 
 // Argument validation shared by every entry point (pipeline.cu:133-141).
 void validate_lof_args(const void* points, int64_t n, int d, int k);

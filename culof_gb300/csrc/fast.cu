@@ -809,6 +809,7 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
     }
     CG_LAUNCH_CHECK();
 
+    mark(2);
     // 3. seed lists, k-th keys and thresholds
     char* rows = static_cast<char*>(rows_.get(padded * (sizeof(uint64_t) * (k + 1) + sizeof(float)) +
                                               static_cast<size_t>(nsplit) * padded * k * sizeof(uint64_t) + 256));
@@ -826,6 +827,7 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
     }
     CG_LAUNCH_CHECK();
 
+    mark(3);
     // 4. sweep over the other tiles, split S ways
     if (nt > 1) {
         const bool big = k > 32;
@@ -842,6 +844,7 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
     }
     const int ns = nt > 1 ? nsplit : 0;
 
+    mark(4);
     // 5. merge into the reference slot order
     const int total = (ns + 1) * k;
     if (total <= 64) launch_merge<2>(seed_keys, partial, perm, n, nt, ns, k, nbr_idx, nbr_d2, kdist2, s);

@@ -100,6 +100,23 @@ CULOF_API int culof_context_fit_predict_device(culof_context* ctx, const float* 
                                      int n_dims, int k, int normalize, double contamination,
                                      float* d_nof, int64_t* d_labels, double* d_offset);
 
+/* Per-stage timing with CUDA events on the context stream (off by default).
+ * culof_context_stage_times writes milliseconds of the last call for up to
+ * cap stages (0 centre+norms, 1 spatial order+tiles, 2 seed, 3 sweep or tile
+ * select, 4 merge, 5 lrd+score, 6 offset+labels; -1 = did not run) and
+ * synchronises the stream. No reference counterpart: measurement support. */
+CULOF_API int culof_context_set_timing(culof_context* ctx, int on);
+CULOF_API int culof_context_stage_times(culof_context* ctx, float* ms, int cap);
+
+/* Kernels launched by this library in this process so far. No reference
+ * counterpart: measurement support. */
+CULOF_API unsigned long long culof_kernel_launch_count(void);
+
+/* Measured FP32 CUDA-core throughput of the current device in TFLOP/s
+ * (packed = 1: fma.rn.f32x2; 0: scalar fma.rn.f32), the roofline
+ * denominator of the FP32 distance sweep. No reference counterpart. */
+CULOF_API int culof_probe_fp32_tflops(int packed, double* tflops_out);
+
 /* ---- stage entry points (the reference's internal stage API) ---------- */
 
 /* include/culof_internal.cuh:63 choose_tile_rows (pipeline.cu:33-38):
