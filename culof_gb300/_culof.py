@@ -77,6 +77,7 @@ _SIGS = {
     "culof_compute_lrd": ([_P, _P, _P, _P, _I64, _I, _P], _I),
     "culof_compute_scores": ([_P, _P, _P, _I64, _I, _P], _I),
     "culof_context_contamination_offset_device": ([_P, _P, _I64, _D, _P], _I),
+    "culof_contamination_offset_noalloc": ([_P, _P, _I64, _D, _P], _I),
 }
 for _name, (_args, _res) in _SIGS.items():
     _fn = getattr(_lib, _name)
@@ -140,6 +141,14 @@ def fit_predict(points, k: int, normalize: bool, contamination):
         )
     )
     return nof, labels, off.value
+
+
+def contamination_offset_noalloc(stream: int, nof: int, n_points: int, contamination, offset: int) -> None:
+    """offset_ of a device nof array into a device double, allocating nothing
+    (culof_contamination_offset_noalloc: for callers that cannot allocate
+    device memory while they run; n_points <= 2^31 - 1; concurrent calls race)."""
+    c = -1.0 if contamination == "auto" else float(contamination)
+    _check(_lib.culof_contamination_offset_noalloc(stream, nof, int(n_points), c, offset))
 
 
 def kernel_launch_count() -> int:

@@ -68,6 +68,11 @@ Engine& engine_of(culof_context* ctx) {
 
 }  // namespace
 
+namespace culof_gb300 {
+// Lets entry points defined in other files report through culof_last_error().
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+}  // namespace culof_gb300
+
 extern "C" {
 
 const char* culof_version(void) { return "0.2.0"; }

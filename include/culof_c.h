@@ -154,6 +154,21 @@ CULOF_API int culof_context_contamination_offset_device(culof_context* ctx, cons
                                               int64_t n_points, double contamination,
                                               double* d_offset);
 
+/* The same offset as culof_context_contamination_offset_device, for callers
+ * that cannot allocate device memory while they run (an operator inside a
+ * framework that owns all device memory through its own pool, a loop that
+ * must not stall on cudaMalloc/cudaFree). It allocates nothing: the caller
+ * passes device buffers for d_nof and d_offset, and the select's scratch is a
+ * fixed 8,232-byte array in this library's device memory, which every GPU
+ * that loads the library holds until the process exits. n_points must be at
+ * most 2^31 - 1 (larger sizes are rejected with CULOF_ERR_INVALID_ARGUMENT).
+ * The first call on a device looks up the array's address (cudaGetSymbolAddress);
+ * make it before any stream capture. Every call shares the array and clears
+ * it first; calls that overlap on the GPU race on it. Asynchronous on
+ * cuda_stream. It has no counterpart in the reference. */
+CULOF_API int culof_contamination_offset_noalloc(void* cuda_stream, const float* d_nof, int64_t n_points,
+                                                 double contamination, double* d_offset);
+
 #ifdef __cplusplus
 }
 #endif
