@@ -49,7 +49,7 @@ L2_FLUSH_BYTES = 256 << 20
 def parse_args():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--steps", type=int, default=30)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--n", type=int, default=200_000)
@@ -100,7 +100,7 @@ class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
 
     QUERY = (
-        "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+        "timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
     )
@@ -121,6 +121,9 @@ class ClockSampler:
         except (OSError, FileNotFoundError):
             self.proc = None
 
+    def window(self, t0: float, t1: float):
+        self.t0, self.t1 = t0, t1
+
     def stop(self):
         if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
@@ -135,7 +138,22 @@ class ClockSampler:
         os.unlink(self.file.name)
         sm, mx, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for r in rows:
+        t0, t1 = getattr(self, "t0", None), getattr(self, "t1", None)
+
+        def in_window(stamp: str) -> bool:
+            if t0 is None:
+                return True
+            try:
+                import datetime
+
+                ts = datetime.datetime.strptime(stamp.strip(), "%Y/%m/%d %H:%M:%S.%f").timestamp()
+            except ValueError:
+                return True
+            return t0 - 0.25 <= ts <= t1 + 0.25
+
+        rows_in = [r for r in rows if r and in_window(r[0])] or rows
+        for r in rows_in:
+            r = r[1:]
             try:
                 sm.append(float(r[1]))
                 mx.append(float(r[2]))
@@ -156,8 +174,8 @@ class ClockSampler:
 
 
 def cpu_sample(args, X, target_s: float):
-    """Oracle k-NN (the dominant cost) over a bounded sample of rows, all host
-    threads, plus the LRD/score pass; returns (pair-dists/s, rows, seconds)."""
+    """Oracle exact k-NN (the dominant cost of the CPU path) over a bounded
+    sample of rows on all host threads; returns (pair-dists/s, rows, seconds)."""
     import oracle
 
     oracle.build()
@@ -265,7 +283,9 @@ def run_ours(args):
 
     sampler = ClockSampler(local)
     sampler.start()
+    time.sleep(1.0)  # nvidia-smi start-up, so samples cover the timed region
     barrier()
+    wall0 = time.time()
     launches0 = _culof.kernel_launch_count()
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
@@ -279,6 +299,7 @@ def run_ours(args):
         for name, ms in ctx.stage_times().items():  # synchronises; outside the events
             stage_acc.setdefault(name, []).append(ms)
     barrier()
+    sampler.window(wall0, time.time())
     launches = _culof.kernel_launch_count() - launches0
     ctx.synchronize()
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
