@@ -10,16 +10,18 @@
 //     are spatially compact.
 //  2. seed: per row, the exact k best over its own tile (warp bitonic sort of
 //     128 exact keys). Its k-th key K bounds the row's true k-th key.
-//  3. sweep: each CTA owns 128 rows (4 per lane, in registers as -2a) and
-//     streams column tiles (TMA bulk copies into shared memory, nearest tiles
-//     first). For every pair it evaluates e = |b|^2 - 2 a.b with packed
-//     fma.rn.f32x2 (two columns per instruction) and compares with a per-row
-//     threshold tau; tau is a rigorous float32 error bound over K, so every
-//     column that can still enter the k best passes. Survivors get their
-//     exact distance (direct differences, the oracle's formula) and, if
-//     their key beats K, are appended to the row's list in shared memory;
-//     full lists are compacted (bitonic sort, dedup, keep k) at block
-//     boundaries, tightening K and tau.
+//  3. sweep: each CTA owns 128 rows and streams column tiles (TMA bulk
+//     copies into shared memory, nearest tiles first); each warp owns 16 of
+//     the rows (4 per lane, in registers as -2a). For every pair it
+//     evaluates e = |b|^2 - 2 a.b with packed fma.rn.f32x2 (two columns per
+//     instruction) and compares with a per-row threshold tau, a rigorous
+//     float32 error bound over the row's current k-th key K, so every column
+//     that can still enter the k best passes. Passing pairs are queued per
+//     warp and rescored 32 at a time (exact distance, the oracle's formula);
+//     keys that beat K join the row's list in shared memory, and filling
+//     lists are compacted (bitonic sort, dedup, keep k), tightening K and
+//     tau. K is shared across the column splits of a row tile through
+//     global memory (atomicMin), so later splits start from earlier ones'.
 //  4. merge: the seed list and the S column-split lists give the k best
 //     keys; slots are written in the reference's order (keys below the k-th
 //     by ascending index, then the ties, knn.cu:190-224).
@@ -55,12 +57,24 @@ constexpr long long kSpinLimit = 1ll << 24;  // bounded mbarrier waits (~1-2 s w
 // ---------------------------------------------------------------- layout
 // Column tile t (kCT consecutive sorted points) in global memory and, when
 // staged, in shared memory:
-//   coords: kPairs x 2*DP floats, pair p = columns (2p, 2p+1) interleaved
-//           per dimension: [b_2p[0], b_2p+1[0], b_2p[1], b_2p+1[1], ...]
+//   coords: kPairs pair records of pair_stride(DP) floats; pair p holds
+//           columns (2p, 2p+1) interleaved per dimension,
+//           [b_2p[0], b_2p+1[0], b_2p[1], b_2p+1[1], ...], then padding so
+//           that eight pair records read by one warp hit distinct banks
 //   norms : kCT floats (NaN for padding columns)
 //   index : kCT uint32 original indices (kNoIndex for padding)
-__host__ __device__ constexpr int tile_floats(int dp) { return kCT * dp + kCT + kCT; }
+// The CTA's own rows are the columns of its own tile.
+__host__ __device__ constexpr int pair_stride(int dp) { return ((2 * dp / 4) % 2 == 1) ? 2 * dp : 2 * dp + 4; }
+__host__ __device__ constexpr int tile_norms_off(int dp) { return kPairs * pair_stride(dp); }
+__host__ __device__ constexpr int tile_index_off(int dp) { return tile_norms_off(dp) + kCT; }
+__host__ __device__ constexpr int tile_floats(int dp) { return tile_index_off(dp) + kCT; }
 __host__ __device__ constexpr int tile_bytes(int dp) { return tile_floats(dp) * 4; }
+
+// Coordinate f of column c within a tile.
+template <int DP>
+__device__ __forceinline__ float tile_coord(const float* tile, int c, int f) {
+    return tile[(c >> 1) * pair_stride(DP) + 2 * f + (c & 1)];
+}
 
 // Column-tile visiting order of row tile T: T, T+1, T-1, T+2, T-2, ... mod nt
 // (a permutation of 0..nt-1); sorted order is spatial, so nearby tiles first.
@@ -318,44 +332,43 @@ __global__ void build_tiles_kernel(const float* __restrict__ xc, const float* __
 #pragma unroll
         for (int f = 0; f < DP; ++f) {
             const float v = (valid && f < d) ? xc[static_cast<int64_t>(orig) * d + f] : 0.0f;
-            tile[pair * 2 * DP + 2 * f + side] = v;
+            tile[pair * pair_stride(DP) + 2 * f + side] = v;
         }
-        tile[kCT * DP + c] = valid ? norms[orig] : __int_as_float(0x7fc00000);
-        reinterpret_cast<unsigned*>(tile)[kCT * DP + kCT + c] = orig;
+        if (side == 0)
+            for (int f = 2 * DP; f < pair_stride(DP); ++f) tile[pair * pair_stride(DP) + f] = 0.0f;
+        tile[tile_norms_off(DP) + c] = valid ? norms[orig] : __int_as_float(0x7fc00000);
+        reinterpret_cast<unsigned*>(tile)[tile_index_off(DP) + c] = orig;
     }
 }
 
 // ---------------------------------------------------------------- seed
 
-// Exact distance between column `ca` and column `cb` of two staged tiles.
+// Exact distance (the oracle's formula) between column ca of tile ta and
+// column cb of tile tb.
 template <int DP>
 __device__ __forceinline__ float tile_dist2(const float* ta, int ca, const float* tb, int cb) {
-    const float* pa = ta + (ca >> 1) * 2 * DP + (ca & 1);
-    const float* pb = tb + (cb >> 1) * 2 * DP + (cb & 1);
     float s = 0.0f;
 #pragma unroll
     for (int f = 0; f < DP; ++f) {
-        const float t = __fsub_rn(pa[2 * f], pb[2 * f]);
+        const float t = __fsub_rn(tile_coord<DP>(ta, ca, f), tile_coord<DP>(tb, cb, f));
         s = __fmaf_rn(t, t, s);
     }
     return s;
 }
 
-// Per row of tile T: the exact k best keys over tile T's own columns
-// (sorted, kKeyMax padded), its k-th key and the filter threshold.
+// Per row of tile T: the exact k best keys over tile T's own columns (sorted,
+// kKeyMax padded) and its k-th key, the starting point of the row's shared
+// k-th key (kth_shared) that the sweep CTAs tighten with atomicMin.
 template <int DP>
 __global__ void __launch_bounds__(kThreads) seed_kernel(const float* __restrict__ tiles, int nt, int64_t n, int k,
-                                                        const unsigned* __restrict__ max_norm_bits,
                                                         uint64_t* __restrict__ seed_keys,
-                                                        uint64_t* __restrict__ seed_kth, float* __restrict__ seed_tau) {
+                                                        unsigned long long* __restrict__ kth_shared) {
     __shared__ __align__(16) float tile[tile_floats(DP)];
     const int T = blockIdx.x;
     const float* src = tiles + static_cast<int64_t>(T) * tile_floats(DP);
     for (int i = threadIdx.x; i < tile_floats(DP); i += kThreads) tile[i] = src[i];
     __syncthreads();
-    const float nmax = __uint_as_float(*max_norm_bits);
-    const unsigned* idx = reinterpret_cast<const unsigned*>(tile + kCT * DP + kCT);
-    const float* nrm = tile + kCT * DP;
+    const unsigned* idx = reinterpret_cast<const unsigned*>(tile + tile_index_off(DP));
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int r = warp; r < kRT; r += kWarps) {
         const int64_t pos = static_cast<int64_t>(T) * kRT + r;
@@ -370,14 +383,11 @@ __global__ void __launch_bounds__(kThreads) seed_kernel(const float* __restrict_
             v[j] = key;
         }
         warp_bitonic_sort<4>(v);
-        uint64_t kth = kKeyMax;
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             const int e = j * 32 + lane;
             if (e < k) seed_keys[pos * k + e] = v[j];
-            if (e == k - 1) kth = v[j];
         }
-        // broadcast kth from its owner lane
         const int owner = (k - 1) & 31, oreg = (k - 1) >> 5;
         uint64_t kk = kKeyMax;
 #pragma unroll
@@ -385,31 +395,31 @@ __global__ void __launch_bounds__(kThreads) seed_kernel(const float* __restrict_
             const uint64_t t = __shfl_sync(0xffffffffu, v[j], owner);
             if (j == oreg) kk = t;
         }
-        (void)kth;
-        if (lane == 0) {
-            seed_kth[pos] = row_valid ? kk : kKeyMax;
-            seed_tau[pos] = row_valid ? tau_from(kk, nrm[r], nmax, DP) : __int_as_float(0xff800000);
-        }
+        if (lane == 0) kth_shared[pos] = row_valid ? kk : kKeyMax;
     }
 }
 
 // ---------------------------------------------------------------- sweep
+
+constexpr int kRowsPerWarp = kRT / kWarps;     // 16 rows owned by each warp
+constexpr int kQueueCap = 32 + 8 * 32;          // one drain chunk + one full step of candidates
 
 template <int DP, int M>
 struct SweepSmem {
     float tiles[kStages][tile_floats(DP)];
     uint64_t list[kRT][M];
     uint64_t kth[kRT];
-    uint64_t bar[kStages];
+    uint64_t full_bar[kStages];
+    float rowc[kRT][DP];
     float tau[kRT];
     float row_norm[kRT];
     int cnt[kRT];
-    int need[2];
-    int abort;
+    int done[kStages];
+    uint16_t queue[kWarps][kQueueCap];
 };
 
-// Compact row r's list: sort, drop duplicates, keep the k smallest; tighten
-// the k-th key (only ever downwards) and tau. Whole warp.
+// Compact row r's list (whole warp): sort, drop duplicates, keep the k
+// smallest, and tighten the row's k-th key (only ever downwards) and tau.
 template <int DP, int M>
 __device__ void compact_row(SweepSmem<DP, M>& sh, int r, int k, float nmax) {
     constexpr int E = M / 32;
@@ -431,76 +441,65 @@ __device__ void compact_row(SweepSmem<DP, M>& sh, int r, int k, float nmax) {
         if (rank[j] >= 0 && rank[j] < k) sh.list[r][rank[j]] = v[j];
         if (rank[j] == k - 1) kth_new = v[j];
     }
-    // the lane that holds rank k-1 (if any) publishes the new k-th key
     const unsigned m = __ballot_sync(0xffffffffu, kth_new != kKeyMax);
+    const uint64_t kk = __shfl_sync(0xffffffffu, kth_new, m ? __ffs(m) - 1 : 0);
     __syncwarp();
-    if (lane == 0) sh.cnt[r] = min(uniq, k);
-    if (m) {
-        const int src = __ffs(m) - 1;
-        const uint64_t kk = __shfl_sync(0xffffffffu, kth_new, src);
-        if (lane == 0 && kk < sh.kth[r]) {
+    if (lane == 0) {
+        sh.cnt[r] = min(uniq, k);
+        if (m && kk < sh.kth[r]) {
             sh.kth[r] = kk;
             sh.tau[r] = tau_from(kk, sh.row_norm[r], nmax, DP);
         }
-    } else {
-        __shfl_sync(0xffffffffu, kth_new, 0);
     }
     __syncwarp();
 }
 
-// Re-run one row against a range of tiles of its visiting order, exactly,
-// reading column tiles from global memory (after a list overflow).
+// Exact rescoring of the warp's queued candidates (one per lane): exact
+// distance, append to the row list if the key beats the row's k-th key;
+// rows that are filling up are compacted after every chunk of 32 (so a list
+// never overflows: M >= k + 32). Returns true if any row was compacted.
 template <int DP, int M>
-__device__ void redo_row(SweepSmem<DP, M>& sh, int r, int k, float nmax, const float* __restrict__ tiles,
-                         const float* __restrict__ own_tile, int T, int nt, int split, int nsplit, int m_begin,
-                         int m_end) {
-    const int lane = threadIdx.x & 31;
-    float a[DP];
+__device__ bool drain_queue(SweepSmem<DP, M>& sh, int qc, const float* __restrict__ tl, int k, float nmax) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const unsigned* tidx = reinterpret_cast<const unsigned*>(tl + tile_index_off(DP));
+    bool compacted = false;
+    for (int base = 0; base < qc; base += 32) {
+        const int i = base + lane;
+        if (i < qc) {
+            const unsigned e = sh.queue[warp][i];
+            const int r = static_cast<int>(e >> 8), c = static_cast<int>(e & 0xFF);
+            float s = 0.0f;
 #pragma unroll
-    for (int f = 0; f < DP; ++f) a[f] = own_tile[(r >> 1) * 2 * DP + 2 * f + (r & 1)];
-    for (int m = m_begin; m < m_end; ++m) {
-        const int q = 1 + split + m * nsplit;
-        const float* tg = tiles + static_cast<int64_t>(spiral_tile(T, q, nt)) * tile_floats(DP);
-        const unsigned* idx = reinterpret_cast<const unsigned*>(tg + kCT * DP + kCT);
-        for (int c0 = 0; c0 < kCT; c0 += 32) {
-            const int c = c0 + lane;
-            const unsigned ci = idx[c];
-            bool take = false;
-            uint64_t key = kKeyMax;
-            if (ci != kNoIndex) {
-                const float* pb = tg + (c >> 1) * 2 * DP + (c & 1);
-                float s = 0.0f;
-#pragma unroll
-                for (int f = 0; f < DP; ++f) {
-                    const float t = __fsub_rn(a[f], pb[2 * f]);
-                    s = __fmaf_rn(t, t, s);
-                }
-                key = make_key(__float_as_uint(s), ci);
-                take = key < sh.kth[r];
+            for (int f = 0; f < DP; ++f) {
+                const float t = __fsub_rn(sh.rowc[r][f], tile_coord<DP>(tl, c, f));
+                s = __fmaf_rn(t, t, s);
             }
-            const unsigned mask = __ballot_sync(0xffffffffu, take);
-            if (mask == 0) continue;
-            int base = sh.cnt[r];
-            if (base + __popc(mask) > M) {
-                __syncwarp();
-                compact_row<DP, M>(sh, r, k, nmax);
-                base = sh.cnt[r];
-                take = take && key < sh.kth[r];
+            const uint64_t key = make_key(__float_as_uint(s), tidx[c]);
+            if (key < sh.kth[r]) {
+                const int slot = atomicAdd(&sh.cnt[r], 1);
+                sh.list[r][slot] = key;
             }
-            const unsigned m2 = __ballot_sync(0xffffffffu, take);
-            if (take) sh.list[r][base + __popc(m2 & ((1u << lane) - 1u))] = key;
-            __syncwarp();
-            if (lane == 0) sh.cnt[r] = base + __popc(m2);
-            __syncwarp();
+        }
+        __syncwarp();
+        const int row0 = warp * kRowsPerWarp;
+        unsigned full = __ballot_sync(0xffffffffu, lane < kRowsPerWarp && sh.cnt[row0 + lane] > M - 32);
+        compacted |= full != 0;
+        while (full) {
+            compact_row<DP, M>(sh, row0 + __ffs(full) - 1, k, nmax);
+            full &= full - 1;
         }
     }
+    return compacted;
 }
 
+// One CTA per (row tile T, split): the rows of T against the split's share
+// of the other column tiles. Each warp owns 16 rows (their lists, k-th keys
+// and thresholds), so list maintenance needs no block barrier; column tiles
+// arrive by TMA and the last warp to finish a tile refills its stage.
 template <int DP, int M>
 __global__ void __launch_bounds__(kThreads, 2)
 sweep_kernel(const float* __restrict__ tiles, int nt, int nsplit, int k, const unsigned* __restrict__ max_norm_bits,
-             const uint64_t* __restrict__ seed_kth, const float* __restrict__ seed_tau,
-             uint64_t* __restrict__ partial, int* __restrict__ status) {
+             unsigned long long* __restrict__ kth_shared, uint64_t* __restrict__ partial, int* __restrict__ status) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     SweepSmem<DP, M>& sh = *reinterpret_cast<SweepSmem<DP, M>*>(smem_raw);
     const int T = blockIdx.x % nt;
@@ -508,144 +507,158 @@ sweep_kernel(const float* __restrict__ tiles, int nt, int nsplit, int k, const u
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const float nmax = __uint_as_float(*max_norm_bits);
     const float* own = tiles + static_cast<int64_t>(T) * tile_floats(DP);
-    // tiles of this split: visiting positions q = 1 + split + m * nsplit
-    const int count = (nt - 1 - split + nsplit - 1) / nsplit > 0 ? (nt - 1 - split + nsplit - 1) / nsplit : 0;
+    // this split's contiguous run of visiting positions q in [q0, q1), q >= 1
+    const int per = (nt - 1 + nsplit - 1) / nsplit;
+    const int q0 = 1 + split * per;
+    const int q1 = min(nt, q0 + per);
+    const int count = q1 > q0 ? q1 - q0 : 0;
     constexpr unsigned kTileBytes = tile_bytes(DP);
 
     if (tid < kRT) {
         const int64_t pos = static_cast<int64_t>(T) * kRT + tid;
-        sh.kth[tid] = seed_kth[pos];
-        sh.tau[tid] = seed_tau[pos];
-        sh.row_norm[tid] = own[kCT * DP + tid];
+        const float nr = own[tile_norms_off(DP) + tid];
+        const uint64_t kk = kth_shared[pos];
+        sh.kth[tid] = kk;
+        sh.row_norm[tid] = nr;
+        sh.tau[tid] = (reinterpret_cast<const unsigned*>(own)[tile_index_off(DP) + tid] == kNoIndex)
+                          ? __int_as_float(0xff800000)
+                          : tau_from(kk, nr, nmax, DP);
         sh.cnt[tid] = 0;
+#pragma unroll
+        for (int f = 0; f < DP; ++f) sh.rowc[tid][f] = tile_coord<DP>(own, tid, f);
     }
+    if (tid < kStages) sh.done[tid] = 0;
     if (tid == 0) {
-        sh.need[0] = sh.need[1] = 0;
-        sh.abort = 0;
-        for (int s = 0; s < kStages; ++s) mbar_init(&sh.bar[s], 1);
+        for (int s = 0; s < kStages; ++s) mbar_init(&sh.full_bar[s], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
     if (tid == 0) {
         for (int m = 0; m < kStages && m < count; ++m) {
-            const int t = spiral_tile(T, 1 + split + m * nsplit, nt);
-            mbar_expect_tx(&sh.bar[m], kTileBytes);
-            tma_load_1d(sh.tiles[m], tiles + static_cast<int64_t>(t) * tile_floats(DP), kTileBytes, &sh.bar[m]);
+            const int t = spiral_tile(T, q0 + m, nt);
+            mbar_expect_tx(&sh.full_bar[m], kTileBytes);
+            tma_load_1d(sh.tiles[m], tiles + static_cast<int64_t>(t) * tile_floats(DP), kTileBytes, &sh.full_bar[m]);
         }
     }
-    // this lane's rows: r = lane * 4 + j, held as dup(-2 a) per dimension
+    // lane = (row group g, pair slot cp): rows warp*16 + g*4 + j, pairs s*8 + cp
+    const int g = lane >> 3, cp = lane & 7;
+    const int rbase = warp * kRowsPerWarp + g * kRowsPerLane;
     uint64_t a2[kRowsPerLane][DP];
     float tau_r[kRowsPerLane];
 #pragma unroll
     for (int j = 0; j < kRowsPerLane; ++j) {
-        const int r = lane * kRowsPerLane + j;
 #pragma unroll
-        for (int f = 0; f < DP; ++f) a2[j][f] = dup2(-2.0f * own[(r >> 1) * 2 * DP + 2 * f + (r & 1)]);
-        tau_r[j] = sh.tau[r];
+        for (int f = 0; f < DP; ++f) a2[j][f] = dup2(-2.0f * sh.rowc[rbase + j][f]);
+        tau_r[j] = sh.tau[rbase + j];
     }
 
-    int parity = 0;
-    bool ok = true, aborted = false;
-    for (int m0 = 0; m0 < count; m0 += kBlockTiles) {
-        const int m1 = min(count, m0 + kBlockTiles);
-        for (int m = m0; m < m1; ++m) {
-            const int stage = m % kStages;
-            if (!mbar_wait(&sh.bar[stage], (m / kStages) & 1)) ok = false;
-            const float* tl = sh.tiles[stage];
-            const float* tn = tl + kCT * DP;
-            const unsigned* ti = reinterpret_cast<const unsigned*>(tl + kCT * DP + kCT);
-#pragma unroll 1
-            for (int p = warp; p < kPairs; p += kWarps) {
-                uint64_t B[DP];
-#pragma unroll
-                for (int f = 0; f < DP; f += 2) {
-                    const ulonglong2 v = *reinterpret_cast<const ulonglong2*>(tl + p * 2 * DP + 2 * f);
-                    B[f] = v.x;
-                    B[f + 1] = v.y;
-                }
-                const uint64_t nb = *reinterpret_cast<const uint64_t*>(tn + 2 * p);
-                uint64_t e[kRowsPerLane];
-                bool any = false;
-#pragma unroll
-                for (int j = 0; j < kRowsPerLane; ++j) {
-                    uint64_t acc = nb;
-#pragma unroll
-                    for (int f = 0; f < DP; ++f) acc = fma2(a2[j][f], B[f], acc);
-                    e[j] = acc;
-                    any |= (lo_f(acc) <= tau_r[j]) | (hi_f(acc) <= tau_r[j]);
-                }
-                if (__any_sync(0xffffffffu, any)) {
-                    // Slow path: exact distance for each passing pair, append if it beats the k-th key.
-#pragma unroll
-                    for (int j = 0; j < kRowsPerLane; ++j) {
-#pragma unroll
-                        for (int side = 0; side < 2; ++side) {
-                            const float ev = side ? hi_f(e[j]) : lo_f(e[j]);
-                            if (!(ev <= tau_r[j])) continue;
-                            const int r = lane * kRowsPerLane + j;
-                            float s = 0.0f;
-#pragma unroll
-                            for (int f = 0; f < DP; ++f) {
-                                const float af = -0.5f * lo_f(a2[j][f]);
-                                const float bf = side ? hi_f(B[f]) : lo_f(B[f]);
-                                const float t = __fsub_rn(af, bf);
-                                s = __fmaf_rn(t, t, s);
-                            }
-                            const unsigned ci = ti[2 * p + side];
-                            const uint64_t key = make_key(__float_as_uint(s), ci);
-                            if (ci != kNoIndex && key < sh.kth[r]) {
-                                const int slot = atomicAdd(&sh.cnt[r], 1);
-                                if (slot < M) sh.list[r][slot] = key;
-                                if (slot >= M - kPairs / 2) sh.need[parity] = 1;
-                            }
-                        }
-                    }
-                }
-            }
-        }
-        // ---- boundary: all warps are done with tiles m0..m1-1 (and agree on failure)
-        const int failed = __syncthreads_or(ok ? 0 : 1);
-        if (tid == 0) {
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            for (int m = m0 + kStages; m < m1 + kStages && m < count; ++m) {
-                const int stage = m % kStages;
-                const int t = spiral_tile(T, 1 + split + m * nsplit, nt);
-                mbar_expect_tx(&sh.bar[stage], kTileBytes);
-                tma_load_1d(sh.tiles[stage], tiles + static_cast<int64_t>(t) * tile_floats(DP), kTileBytes,
-                            &sh.bar[stage]);
-            }
-        }
-        if (sh.need[parity]) {
-            for (int r = warp; r < kRT; r += kWarps) {
-                const int c = sh.cnt[r];
-                if (c >= M - kPairs / 2) {
-                    compact_row<DP, M>(sh, r, k, nmax);
-                    if (c > M) redo_row<DP, M>(sh, r, k, nmax, tiles, own, T, nt, split, nsplit, m0, m1);
-                }
-            }
-            __syncthreads();
-            if (tid == 0) sh.need[parity] = 0;
-#pragma unroll
-            for (int j = 0; j < kRowsPerLane; ++j) tau_r[j] = sh.tau[lane * kRowsPerLane + j];
-        }
-        parity ^= 1;
-        if (failed) {
-            aborted = true;
+    bool ok = true;
+    for (int m = 0; m < count && ok; ++m) {
+        const int stage = m % kStages;
+        if (!mbar_wait(&sh.full_bar[stage], (m / kStages) & 1)) {
+            ok = false;
             break;
         }
+        const float* tl = sh.tiles[stage];
+        const float* tn = tl + tile_norms_off(DP);
+        int qc = 0;
+#pragma unroll 1
+        for (int s = 0; s < kPairs / 8; ++s) {
+            const int p = s * 8 + cp;
+            uint64_t B[DP];
+#pragma unroll
+            for (int f = 0; f < DP; f += 2) {
+                const ulonglong2 v = *reinterpret_cast<const ulonglong2*>(tl + p * pair_stride(DP) + 2 * f);
+                B[f] = v.x;
+                B[f + 1] = v.y;
+            }
+            const uint64_t nb = *reinterpret_cast<const uint64_t*>(tn + 2 * p);
+            uint64_t acc[kRowsPerLane];
+#pragma unroll
+            for (int j = 0; j < kRowsPerLane; ++j) acc[j] = nb;
+#pragma unroll
+            for (int f = 0; f < DP; ++f) {
+#pragma unroll
+                for (int j = 0; j < kRowsPerLane; ++j) acc[j] = fma2(a2[j][f], B[f], acc[j]);
+            }
+            unsigned pass = 0;
+#pragma unroll
+            for (int j = 0; j < kRowsPerLane; ++j) {
+                pass |= (lo_f(acc[j]) <= tau_r[j] ? 1u : 0u) << (2 * j);
+                pass |= (hi_f(acc[j]) <= tau_r[j] ? 1u : 0u) << (2 * j + 1);
+            }
+            if (__any_sync(0xffffffffu, pass != 0)) {
+                // queue (row, column) of every passing pair; warp-ordered slots
+                const int cntp = __popc(pass);
+                int off = cntp;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int y = __shfl_up_sync(0xffffffffu, off, o);
+                    if (lane >= o) off += y;
+                }
+                const int tot = __shfl_sync(0xffffffffu, off, 31);
+                off -= cntp;
+                while (pass) {
+                    const int b = __ffs(pass) - 1;
+                    pass &= pass - 1;
+                    const int r = rbase + (b >> 1);
+                    const int c = 2 * p + (b & 1);
+                    sh.queue[warp][qc + off++] = static_cast<uint16_t>((r << 8) | c);
+                }
+                qc += tot;
+                __syncwarp();
+                if (qc >= 32) {
+                    if (drain_queue<DP, M>(sh, qc, tl, k, nmax)) {
+#pragma unroll
+                        for (int j = 0; j < kRowsPerLane; ++j) tau_r[j] = sh.tau[rbase + j];
+                    }
+                    qc = 0;
+                }
+            }
+        }
+        if (qc > 0) {
+            if (drain_queue<DP, M>(sh, qc, tl, k, nmax)) {
+#pragma unroll
+                for (int j = 0; j < kRowsPerLane; ++j) tau_r[j] = sh.tau[rbase + j];
+            }
+        }
+        // done with this stage; the last warp out refills it with tile m + kStages
+        __syncwarp();
+        if (lane == 0) {
+            __threadfence_block();
+            const int prev = atomicAdd(&sh.done[stage], 1);
+            if (prev == kWarps - 1) {
+                sh.done[stage] = 0;
+                if (m + kStages < count) {
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                    const int t = spiral_tile(T, q0 + m + kStages, nt);
+                    mbar_expect_tx(&sh.full_bar[stage], kTileBytes);
+                    tma_load_1d(sh.tiles[stage], tiles + static_cast<int64_t>(t) * tile_floats(DP), kTileBytes,
+                                &sh.full_bar[stage]);
+                }
+            }
+        }
     }
-    __syncthreads();
-    if (aborted) {
+    const int failed = __syncthreads_or(ok ? 0 : 1);
+    if (failed) {
         if (tid == 0) atomicExch(status, 1);
-        return;  // copies in flight complete into this CTA's shared memory; nothing else waits on them
+        // wait (bounded) for this CTA's copies still in flight before exiting
+        if (tid < kStages) {
+            for (int m = count - 1; m >= 0 && m >= count - kStages; --m)
+                if (m % kStages == tid) mbar_wait(&sh.full_bar[tid], (m / kStages) & 1);
+        }
+        __syncthreads();
+        return;
     }
-    // ---- final: sorted k best of this split per row
-    for (int r = warp; r < kRT; r += kWarps) {
+    // final: this split's sorted k best per row; share the k-th key
+    for (int i = 0; i < kRowsPerWarp; ++i) {
+        const int r = warp * kRowsPerWarp + i;
         compact_row<DP, M>(sh, r, k, nmax);
         const int64_t pos = static_cast<int64_t>(T) * kRT + r;
         const int c = sh.cnt[r];
         uint64_t* out = partial + (static_cast<int64_t>(split) * nt * kRT + pos) * k;
         for (int e = lane; e < k; e += 32) out[e] = e < c ? sh.list[r][e] : kKeyMax;
+        if (lane == 0 && sh.kth[r] != kKeyMax) atomicMin(&kth_shared[pos], static_cast<unsigned long long>(sh.kth[r]));
     }
 }
 
@@ -713,14 +726,9 @@ int grid_for(int64_t items, int block) {
     return static_cast<int>(g < 1 ? 1 : g);
 }
 
-template <int DP, int M>
-size_t sweep_smem() {
-    return sizeof(SweepSmem<DP, M>);
-}
-
 int choose_splits(int nt, int sms) {
-    // enough CTAs (2 per SM resident) for >= ~8 waves, at most 7 splits
-    const int want = (16 * sms + nt - 1) / nt;
+    // enough CTAs (2 per SM resident) for ~16 waves, at most 7 splits
+    const int want = (32 * sms + nt - 1) / nt;
     int s = want < 1 ? 1 : want;
     if (s > 7) s = 7;
     if (s > nt - 1) s = nt - 1 > 0 ? nt - 1 : 1;
@@ -728,16 +736,16 @@ int choose_splits(int nt, int sms) {
 }
 
 template <int DP, int M>
-void launch_sweep(const float* tiles, int nt, int nsplit, int k, const unsigned* maxn, const uint64_t* skth,
-                  const float* stau, uint64_t* partial, int* status, cudaStream_t s) {
-    const size_t smem = sweep_smem<DP, M>();
-    static bool configured = false;  // per instantiation; attribute set once per process
+void launch_sweep(const float* tiles, int nt, int nsplit, int k, const unsigned* maxn, unsigned long long* kth_shared,
+                  uint64_t* partial, int* status, cudaStream_t s) {
+    const size_t smem = sizeof(SweepSmem<DP, M>);
+    static bool configured = false;  // per instantiation; the attribute is set once per process
     if (!configured) {
         CG_CUDA(cudaFuncSetAttribute(sweep_kernel<DP, M>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      static_cast<int>(smem)));
         configured = true;
     }
-    sweep_kernel<DP, M><<<nt * nsplit, kThreads, smem, s>>>(tiles, nt, nsplit, k, maxn, skth, stau, partial, status);
+    sweep_kernel<DP, M><<<nt * nsplit, kThreads, smem, s>>>(tiles, nt, nsplit, k, maxn, kth_shared, partial, status);
     CG_LAUNCH_CHECK();
 }
 
@@ -799,8 +807,13 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
     const unsigned* perm = vin;  // after 4 passes: back in the first half
 
     // 2. column tiles
-    const size_t tfl = static_cast<size_t>(kCT) * dp + 2 * kCT;
-    float* tiles = cols_.as<float>(tfl * nt);
+    float* tiles = nullptr;
+    switch (dp) {
+        case 2: tiles = cols_.as<float>(static_cast<size_t>(tile_floats(2)) * nt); break;
+        case 4: tiles = cols_.as<float>(static_cast<size_t>(tile_floats(4)) * nt); break;
+        case 6: tiles = cols_.as<float>(static_cast<size_t>(tile_floats(6)) * nt); break;
+        default: tiles = cols_.as<float>(static_cast<size_t>(tile_floats(8)) * nt); break;
+    }
     switch (dp) {
         case 2: build_tiles_kernel<2><<<grid_for(padded, 256), 256, 0, s>>>(xc, norms, n, d, perm, padded, tiles); break;
         case 4: build_tiles_kernel<4><<<grid_for(padded, 256), 256, 0, s>>>(xc, norms, n, d, perm, padded, tiles); break;
@@ -809,31 +822,30 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
     }
     CG_LAUNCH_CHECK();
 
-    mark(2);
-    // 3. seed lists, k-th keys and thresholds
-    char* rows = static_cast<char*>(rows_.get(padded * (sizeof(uint64_t) * (k + 1) + sizeof(float)) +
+    // 3. seed lists and the shared k-th keys
+    char* rows = static_cast<char*>(rows_.get(padded * sizeof(uint64_t) * (k + 1) +
                                               static_cast<size_t>(nsplit) * padded * k * sizeof(uint64_t) + 256));
     uint64_t* seed_keys = reinterpret_cast<uint64_t*>(rows);
-    uint64_t* seed_kth = seed_keys + padded * k;
-    uint64_t* partial = seed_kth + padded;
-    float* seed_tau = reinterpret_cast<float*>(partial + static_cast<size_t>(nsplit) * padded * k);
+    unsigned long long* kth_shared = reinterpret_cast<unsigned long long*>(seed_keys + padded * k);
+    uint64_t* partial = reinterpret_cast<uint64_t*>(kth_shared + padded);
     int* status = status_ptr();
     const unsigned* maxn = reinterpret_cast<const unsigned*>(max_norm_.get(sizeof(unsigned)));
+    mark(2);
     switch (dp) {
-        case 2: seed_kernel<2><<<nt, kThreads, 0, s>>>(tiles, nt, n, k, maxn, seed_keys, seed_kth, seed_tau); break;
-        case 4: seed_kernel<4><<<nt, kThreads, 0, s>>>(tiles, nt, n, k, maxn, seed_keys, seed_kth, seed_tau); break;
-        case 6: seed_kernel<6><<<nt, kThreads, 0, s>>>(tiles, nt, n, k, maxn, seed_keys, seed_kth, seed_tau); break;
-        default: seed_kernel<8><<<nt, kThreads, 0, s>>>(tiles, nt, n, k, maxn, seed_keys, seed_kth, seed_tau); break;
+        case 2: seed_kernel<2><<<nt, kThreads, 0, s>>>(tiles, nt, n, k, seed_keys, kth_shared); break;
+        case 4: seed_kernel<4><<<nt, kThreads, 0, s>>>(tiles, nt, n, k, seed_keys, kth_shared); break;
+        case 6: seed_kernel<6><<<nt, kThreads, 0, s>>>(tiles, nt, n, k, seed_keys, kth_shared); break;
+        default: seed_kernel<8><<<nt, kThreads, 0, s>>>(tiles, nt, n, k, seed_keys, kth_shared); break;
     }
     CG_LAUNCH_CHECK();
-
     mark(3);
+
     // 4. sweep over the other tiles, split S ways
     if (nt > 1) {
         const bool big = k > 32;
-#define CG_SWEEP(DPV)                                                                                          \
-    (big ? launch_sweep<DPV, 128>(tiles, nt, nsplit, k, maxn, seed_kth, seed_tau, partial, status, s)         \
-         : launch_sweep<DPV, 64>(tiles, nt, nsplit, k, maxn, seed_kth, seed_tau, partial, status, s))
+#define CG_SWEEP(DPV)                                                                                 \
+    (big ? launch_sweep<DPV, 96>(tiles, nt, nsplit, k, maxn, kth_shared, partial, status, s)          \
+         : launch_sweep<DPV, 64>(tiles, nt, nsplit, k, maxn, kth_shared, partial, status, s))
         switch (dp) {
             case 2: CG_SWEEP(2); break;
             case 4: CG_SWEEP(4); break;
@@ -843,8 +855,8 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
 #undef CG_SWEEP
     }
     const int ns = nt > 1 ? nsplit : 0;
-
     mark(4);
+
     // 5. merge into the reference slot order
     const int total = (ns + 1) * k;
     if (total <= 64) launch_merge<2>(seed_keys, partial, perm, n, nt, ns, k, nbr_idx, nbr_d2, kdist2, s);
