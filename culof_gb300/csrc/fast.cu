@@ -422,7 +422,9 @@ struct SweepSmem {
 // smallest, and tighten the row's k-th key (only ever downwards) and tau.
 template <int DP, int M>
 __device__ void compact_row(SweepSmem<DP, M>& sh, int r, int k, float nmax) {
-    constexpr int E = M / 32;
+    // the bitonic network needs a power of two: pad M/32 registers up (with kKeyMax)
+    constexpr int E = (M / 32) <= 1 ? 1 : (M / 32) <= 2 ? 2 : (M / 32) <= 4 ? 4 : 8;
+    static_assert(M % 32 == 0 && M <= 256, "list capacity");
     const int lane = threadIdx.x & 31;
     const int c = min(sh.cnt[r], M);
     uint64_t v[E];

@@ -13,6 +13,7 @@ __device__ __forceinline__ uint64_t shfl_xor_u64(uint64_t v, int mask) {
 // e = j * 32 + lane (register j of lane `lane`). E must be a power of two.
 template <int E>
 __device__ __forceinline__ void warp_bitonic_sort(uint64_t (&v)[E]) {
+    static_assert(E > 0 && (E & (E - 1)) == 0, "bitonic sort needs a power-of-two size");
     const int lane = threadIdx.x & 31;
     constexpr int N = 32 * E;
 #pragma unroll
