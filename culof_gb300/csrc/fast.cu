@@ -109,6 +109,15 @@ __device__ __forceinline__ uint64_t fma2(uint64_t a, uint64_t b, uint64_t c) {
     asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
     return d;
 }
+__device__ __forceinline__ uint64_t sub2(uint64_t a, uint64_t b) {
+    uint64_t d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+// The next float above t (t itself for +-inf): x <= t  <=>  x < tau_above(t).
+__device__ __forceinline__ float tau_above(float t) {
+    return (isinf(t)) ? t : nextafterf(t, __int_as_float(0x7f800000));
+}
 __device__ __forceinline__ uint64_t dup2(float x) {
     const uint64_t u = __float_as_uint(x);
     return u | (u << 32);
@@ -547,11 +556,13 @@ sweep_kernel(const float* __restrict__ tiles, int nt, int nsplit, int k, const u
     const int rbase = warp * kRowsPerWarp + g * kRowsPerLane;
     uint64_t a2[kRowsPerLane][DP];
     float tau_r[kRowsPerLane];
+    uint64_t tau2[kRowsPerLane];  // dup(next float above tau): e <= tau  <=>  sign(e - tau') set
 #pragma unroll
     for (int j = 0; j < kRowsPerLane; ++j) {
 #pragma unroll
         for (int f = 0; f < DP; ++f) a2[j][f] = dup2(-2.0f * sh.rowc[rbase + j][f]);
         tau_r[j] = sh.tau[rbase + j];
+        tau2[j] = dup2(tau_above(tau_r[j]));
     }
 
     bool ok = true;
@@ -564,7 +575,7 @@ sweep_kernel(const float* __restrict__ tiles, int nt, int nsplit, int k, const u
         const float* tl = sh.tiles[stage];
         const float* tn = tl + tile_norms_off(DP);
         int qc = 0;
-#pragma unroll 1
+#pragma unroll 2
         for (int s = 0; s < kPairs / 8; ++s) {
             const int p = s * 8 + cp;
             uint64_t B[DP];
@@ -583,13 +594,21 @@ sweep_kernel(const float* __restrict__ tiles, int nt, int nsplit, int k, const u
 #pragma unroll
                 for (int j = 0; j < kRowsPerLane; ++j) acc[j] = fma2(a2[j][f], B[f], acc[j]);
             }
-            unsigned pass = 0;
+            // any of the 8 pairs below its row's threshold? One packed subtract per
+            // row and an OR of the sign bits (e - tau' < 0 exactly when e < tau').
+            unsigned signs = 0;
 #pragma unroll
             for (int j = 0; j < kRowsPerLane; ++j) {
-                pass |= (lo_f(acc[j]) <= tau_r[j] ? 1u : 0u) << (2 * j);
-                pass |= (hi_f(acc[j]) <= tau_r[j] ? 1u : 0u) << (2 * j + 1);
+                const uint64_t dlt = sub2(acc[j], tau2[j]);
+                signs |= static_cast<unsigned>(dlt) | static_cast<unsigned>(dlt >> 32);
             }
-            if (__any_sync(0xffffffffu, pass != 0)) {
+            if (__any_sync(0xffffffffu, static_cast<int>(signs) < 0)) {
+                unsigned pass = 0;
+#pragma unroll
+                for (int j = 0; j < kRowsPerLane; ++j) {
+                    pass |= (lo_f(acc[j]) <= tau_r[j] ? 1u : 0u) << (2 * j);
+                    pass |= (hi_f(acc[j]) <= tau_r[j] ? 1u : 0u) << (2 * j + 1);
+                }
                 // queue (row, column) of every passing pair; warp-ordered slots
                 const int cntp = __popc(pass);
                 int off = cntp;
@@ -612,7 +631,10 @@ sweep_kernel(const float* __restrict__ tiles, int nt, int nsplit, int k, const u
                 if (qc >= 32) {
                     if (drain_queue<DP, M>(sh, qc, tl, k, nmax)) {
 #pragma unroll
-                        for (int j = 0; j < kRowsPerLane; ++j) tau_r[j] = sh.tau[rbase + j];
+                        for (int j = 0; j < kRowsPerLane; ++j) {
+                            tau_r[j] = sh.tau[rbase + j];
+                            tau2[j] = dup2(tau_above(tau_r[j]));
+                        }
                     }
                     qc = 0;
                 }
@@ -621,7 +643,10 @@ sweep_kernel(const float* __restrict__ tiles, int nt, int nsplit, int k, const u
         if (qc > 0) {
             if (drain_queue<DP, M>(sh, qc, tl, k, nmax)) {
 #pragma unroll
-                for (int j = 0; j < kRowsPerLane; ++j) tau_r[j] = sh.tau[rbase + j];
+                for (int j = 0; j < kRowsPerLane; ++j) {
+                    tau_r[j] = sh.tau[rbase + j];
+                    tau2[j] = dup2(tau_above(tau_r[j]));
+                }
             }
         }
         // done with this stage; the last warp out refills it with tile m + kStages
