@@ -35,24 +35,21 @@
 #include "common.cuh"
 #include "engine.cuh"
 #include "fast.cuh"
+#include "sweep_common.cuh"
 #include "warp_sort.cuh"
 
 namespace culof_gb300 {
 
 namespace {
 
-constexpr int kRT = 128;       // rows per row tile
-constexpr int kCT = 128;       // columns per column tile
+using namespace sweep;
+
 constexpr int kPairs = kCT / 2;
-constexpr int kThreads = 256;  // 8 warps
-constexpr int kWarps = kThreads / 32;
 constexpr int kRowsPerLane = 4;
 constexpr int kStages = 4;     // column tiles in flight
-constexpr int kBlockTiles = 2; // tiles between list-maintenance boundaries
-constexpr int kMaxK = 64;
-constexpr int kMaxDP = 8;
-constexpr unsigned kNoIndex = 0xFFFFFFFFu;
-constexpr long long kSpinLimit = 1ll << 24;  // bounded mbarrier waits (~1-2 s with backoff)
+constexpr int kMaxDP = 8;      // the small-d sweep; wider points take wide.cu's
+constexpr int kMaxWideD = 128;
+constexpr int kMortonDims = 8;  // Morton key over (up to) the 8 widest dimensions
 
 // ---------------------------------------------------------------- layout
 // Column tile t (kCT consecutive sorted points) in global memory and, when
@@ -76,39 +73,6 @@ __device__ __forceinline__ float tile_coord(const float* tile, int c, int f) {
     return tile[(c >> 1) * pair_stride(DP) + 2 * f + (c & 1)];
 }
 
-// Column-tile visiting order of row tile T: T, T+1, T-1, T+2, T-2, ... mod nt
-// (a permutation of 0..nt-1); sorted order is spatial, so nearby tiles first.
-__device__ __forceinline__ int spiral_tile(int T, int q, int nt) {
-    const int off = (q & 1) ? (q + 1) >> 1 : -(q >> 1);
-    int t = (T + off) % nt;
-    if (t < 0) t += nt;
-    return t;
-}
-
-// Rigorous filter threshold. For a row a with float32 norm Na and any column
-// b whose exact float32 direct-difference distance is <= kthD, the float32
-// FMA chain e = fl(Nb + sum_f (-2 a_f) b_f) satisfies e <= tau_from(...):
-//   D <= kthD  =>  T = |a-b|^2 (real) <= kthD / (1 - (dp+2) u)
-//   e_exact = T - |a|^2 + (Nb - |b|^2),  |a|^2 >= Na (1 - u),  Nb - |b|^2 <= u Nmax
-//   |e - e_exact| <= gamma_{dp+1} (Nb + 2 sum|a_f b_f|) <= gamma (Nmax + 2 sqrt(Na Nmax)(1+u))
-// plus 4u of slack for the double evaluation; rounded up to float.
-__device__ float tau_from(uint64_t kth_key, float na, float nmax, int dp) {
-    if (kth_key == kKeyMax) return __int_as_float(0x7f800000);
-    const double D = static_cast<double>(__uint_as_float(key_bits(kth_key)));
-    const double u = 5.9604644775390625e-08;  // 2^-24
-    const double tm = D / (1.0 - (dp + 2) * u);
-    const double gam = (dp + 1) * u / (1.0 - (dp + 1) * u);
-    const double a = static_cast<double>(na), m = static_cast<double>(nmax);
-    double t = tm - a * (1.0 - u) + u * m + gam * (m + 2.0 * sqrt(a * m) * (1.0 + u));
-    t += 4.0 * u * (tm + a + m) + 1e-30;
-    return __double2float_ru(t);
-}
-
-__device__ __forceinline__ uint64_t fma2(uint64_t a, uint64_t b, uint64_t c) {
-    uint64_t d;
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
-    return d;
-}
 __device__ __forceinline__ uint64_t sub2(uint64_t a, uint64_t b) {
     uint64_t d;
     asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
@@ -117,49 +81,6 @@ __device__ __forceinline__ uint64_t sub2(uint64_t a, uint64_t b) {
 // The next float above t (t itself for +-inf): x <= t  <=>  x < tau_above(t).
 __device__ __forceinline__ float tau_above(float t) {
     return (isinf(t)) ? t : nextafterf(t, __int_as_float(0x7f800000));
-}
-__device__ __forceinline__ uint64_t dup2(float x) {
-    const uint64_t u = __float_as_uint(x);
-    return u | (u << 32);
-}
-__device__ __forceinline__ float lo_f(uint64_t v) { return __uint_as_float(static_cast<uint32_t>(v)); }
-__device__ __forceinline__ float hi_f(uint64_t v) { return __uint_as_float(static_cast<uint32_t>(v >> 32)); }
-
-// ---------------------------------------------------------------- mbarrier / TMA
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
-                 : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-// Bounded wait: returns false (and the caller flags an error) if the phase
-// never completes.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
-    for (long long it = 0; it < kSpinLimit; ++it) {
-        if (mbar_try_wait(bar, parity)) return true;
-        if (it > 64) __nanosleep(64);
-    }
-    return false;
-}
-__device__ __forceinline__ void tma_load_1d(void* smem_dst, const void* gmem_src, unsigned bytes, uint64_t* bar) {
-    asm volatile(
-        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-            smem_u32(smem_dst)),
-        "l"(gmem_src), "r"(bytes), "r"(smem_u32(bar))
-        : "memory");
 }
 
 // ---------------------------------------------------------------- spatial order
@@ -200,25 +121,50 @@ __global__ void minmax_init_kernel(unsigned* mm, int d) {
     }
 }
 
-// 32-bit Morton key: 32/d bits per dimension (d <= 8), interleaved from the
-// most significant bit, over the bounding box of the centred data.
+// The (up to) kMortonDims dimensions with the widest range, widest first
+// (ties by index); one thread.
+__global__ void select_dims_kernel(const unsigned* __restrict__ mm, int d, int* __restrict__ dims) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const int m = d < kMortonDims ? d : kMortonDims;
+    for (int j = 0; j < m; ++j) {
+        int best = -1;
+        float best_span = -1.0f;
+        for (int f = 0; f < d; ++f) {
+            bool taken = false;
+            for (int q = 0; q < j; ++q) taken |= dims[q] == f;
+            if (taken) continue;
+            const float span = unflip_float(mm[2 * f + 1]) - unflip_float(mm[2 * f]);
+            if (span > best_span) {
+                best_span = span;
+                best = f;
+            }
+        }
+        dims[j] = best;
+    }
+}
+
+// 32-bit Morton key: 32/m bits for each of the m selected dimensions,
+// interleaved from the most significant bit, over the bounding box of the
+// centred data.
 __global__ void morton_kernel(const float* __restrict__ xc, int64_t n, int d, const unsigned* __restrict__ mm,
-                              unsigned* __restrict__ keys, unsigned* __restrict__ vals) {
-    const int bits = (32 / d) < 30 ? (32 / d) : 30;
+                              const int* __restrict__ dims, unsigned* __restrict__ keys, unsigned* __restrict__ vals) {
+    const int md = d < kMortonDims ? d : kMortonDims;
+    const int bits = (32 / md) < 30 ? (32 / md) : 30;
     for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
          i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-        unsigned q[kMaxDP];
-        for (int f = 0; f < d; ++f) {
+        unsigned q[kMortonDims];
+        for (int j = 0; j < md; ++j) {
+            const int f = dims[j];
             const float lo = unflip_float(mm[2 * f]), hi = unflip_float(mm[2 * f + 1]);
             const float span = hi - lo;
             float t = span > 0.0f ? (xc[i * d + f] - lo) / span : 0.0f;
             t = fminf(fmaxf(t, 0.0f), 1.0f);
             const float scale = static_cast<float>((1u << bits) - 1u);
-            q[f] = static_cast<unsigned>(t * scale + 0.5f);
+            q[j] = static_cast<unsigned>(t * scale + 0.5f);
         }
         unsigned key = 0u;
         for (int b = bits - 1; b >= 0; --b)
-            for (int f = 0; f < d; ++f) key = (key << 1) | ((q[f] >> b) & 1u);
+            for (int j = 0; j < md; ++j) key = (key << 1) | ((q[j] >> b) & 1u);
         keys[i] = key;
         vals[i] = static_cast<unsigned>(i);
     }
@@ -410,60 +356,15 @@ __global__ void __launch_bounds__(kThreads) seed_kernel(const float* __restrict_
 
 // ---------------------------------------------------------------- sweep
 
-constexpr int kRowsPerWarp = kRT / kWarps;     // 16 rows owned by each warp
-constexpr int kQueueCap = 32 + 8 * 32;          // one drain chunk + one full step of candidates
-
 template <int DP, int M>
 struct SweepSmem {
     float tiles[kStages][tile_floats(DP)];
-    uint64_t list[kRT][M];
-    uint64_t kth[kRT];
+    RowLists<M> L;
     uint64_t full_bar[kStages];
     float rowc[kRT][DP];
-    float tau[kRT];
-    float row_norm[kRT];
-    int cnt[kRT];
     int done[kStages];
     uint16_t queue[kWarps][kQueueCap];
 };
-
-// Compact row r's list (whole warp): sort, drop duplicates, keep the k
-// smallest, and tighten the row's k-th key (only ever downwards) and tau.
-template <int DP, int M>
-__device__ void compact_row(SweepSmem<DP, M>& sh, int r, int k, float nmax) {
-    // the bitonic network needs a power of two: pad M/32 registers up (with kKeyMax)
-    constexpr int E = (M / 32) <= 1 ? 1 : (M / 32) <= 2 ? 2 : (M / 32) <= 4 ? 4 : 8;
-    static_assert(M % 32 == 0 && M <= 256, "list capacity");
-    const int lane = threadIdx.x & 31;
-    const int c = min(sh.cnt[r], M);
-    uint64_t v[E];
-#pragma unroll
-    for (int j = 0; j < E; ++j) {
-        const int e = j * 32 + lane;
-        v[j] = e < c ? sh.list[r][e] : kKeyMax;
-    }
-    warp_bitonic_sort<E>(v);
-    int rank[E];
-    const int uniq = warp_unique_ranks<E>(v, kKeyMax, rank);
-    __syncwarp();
-    uint64_t kth_new = kKeyMax;
-#pragma unroll
-    for (int j = 0; j < E; ++j) {
-        if (rank[j] >= 0 && rank[j] < k) sh.list[r][rank[j]] = v[j];
-        if (rank[j] == k - 1) kth_new = v[j];
-    }
-    const unsigned m = __ballot_sync(0xffffffffu, kth_new != kKeyMax);
-    const uint64_t kk = __shfl_sync(0xffffffffu, kth_new, m ? __ffs(m) - 1 : 0);
-    __syncwarp();
-    if (lane == 0) {
-        sh.cnt[r] = min(uniq, k);
-        if (m && kk < sh.kth[r]) {
-            sh.kth[r] = kk;
-            sh.tau[r] = tau_from(kk, sh.row_norm[r], nmax, DP);
-        }
-    }
-    __syncwarp();
-}
 
 // Exact rescoring of the warp's queued candidates (one per lane): exact
 // distance, append to the row list if the key beats the row's k-th key;
@@ -486,19 +387,13 @@ __device__ bool drain_queue(SweepSmem<DP, M>& sh, int qc, const float* __restric
                 s = __fmaf_rn(t, t, s);
             }
             const uint64_t key = make_key(__float_as_uint(s), tidx[c]);
-            if (key < sh.kth[r]) {
-                const int slot = atomicAdd(&sh.cnt[r], 1);
-                sh.list[r][slot] = key;
+            if (key < sh.L.kth[r]) {
+                const int slot = atomicAdd(&sh.L.cnt[r], 1);
+                sh.L.list[r][slot] = key;
             }
         }
         __syncwarp();
-        const int row0 = warp * kRowsPerWarp;
-        unsigned full = __ballot_sync(0xffffffffu, lane < kRowsPerWarp && sh.cnt[row0 + lane] > M - 32);
-        compacted |= full != 0;
-        while (full) {
-            compact_row<DP, M>(sh, row0 + __ffs(full) - 1, k, nmax);
-            full &= full - 1;
-        }
+        compacted |= compact_full_rows<M>(sh.L, k, nmax, DP);
     }
     return compacted;
 }
@@ -529,12 +424,12 @@ sweep_kernel(const float* __restrict__ tiles, int nt, int nsplit, int k, const u
         const int64_t pos = static_cast<int64_t>(T) * kRT + tid;
         const float nr = own[tile_norms_off(DP) + tid];
         const uint64_t kk = kth_shared[pos];
-        sh.kth[tid] = kk;
-        sh.row_norm[tid] = nr;
-        sh.tau[tid] = (reinterpret_cast<const unsigned*>(own)[tile_index_off(DP) + tid] == kNoIndex)
+        sh.L.kth[tid] = kk;
+        sh.L.row_norm[tid] = nr;
+        sh.L.tau[tid] = (reinterpret_cast<const unsigned*>(own)[tile_index_off(DP) + tid] == kNoIndex)
                           ? __int_as_float(0xff800000)
                           : tau_from(kk, nr, nmax, DP);
-        sh.cnt[tid] = 0;
+        sh.L.cnt[tid] = 0;
 #pragma unroll
         for (int f = 0; f < DP; ++f) sh.rowc[tid][f] = tile_coord<DP>(own, tid, f);
     }
@@ -561,7 +456,7 @@ sweep_kernel(const float* __restrict__ tiles, int nt, int nsplit, int k, const u
     for (int j = 0; j < kRowsPerLane; ++j) {
 #pragma unroll
         for (int f = 0; f < DP; ++f) a2[j][f] = dup2(-2.0f * sh.rowc[rbase + j][f]);
-        tau_r[j] = sh.tau[rbase + j];
+        tau_r[j] = sh.L.tau[rbase + j];
         tau2[j] = dup2(tau_above(tau_r[j]));
     }
 
@@ -632,7 +527,7 @@ sweep_kernel(const float* __restrict__ tiles, int nt, int nsplit, int k, const u
                     if (drain_queue<DP, M>(sh, qc, tl, k, nmax)) {
 #pragma unroll
                         for (int j = 0; j < kRowsPerLane; ++j) {
-                            tau_r[j] = sh.tau[rbase + j];
+                            tau_r[j] = sh.L.tau[rbase + j];
                             tau2[j] = dup2(tau_above(tau_r[j]));
                         }
                     }
@@ -644,7 +539,7 @@ sweep_kernel(const float* __restrict__ tiles, int nt, int nsplit, int k, const u
             if (drain_queue<DP, M>(sh, qc, tl, k, nmax)) {
 #pragma unroll
                 for (int j = 0; j < kRowsPerLane; ++j) {
-                    tau_r[j] = sh.tau[rbase + j];
+                    tau_r[j] = sh.L.tau[rbase + j];
                     tau2[j] = dup2(tau_above(tau_r[j]));
                 }
             }
@@ -680,12 +575,12 @@ sweep_kernel(const float* __restrict__ tiles, int nt, int nsplit, int k, const u
     // final: this split's sorted k best per row; share the k-th key
     for (int i = 0; i < kRowsPerWarp; ++i) {
         const int r = warp * kRowsPerWarp + i;
-        compact_row<DP, M>(sh, r, k, nmax);
+        compact_row<M>(sh.L, r, k, nmax, DP);
         const int64_t pos = static_cast<int64_t>(T) * kRT + r;
-        const int c = sh.cnt[r];
+        const int c = sh.L.cnt[r];
         uint64_t* out = partial + (static_cast<int64_t>(split) * nt * kRT + pos) * k;
-        for (int e = lane; e < k; e += 32) out[e] = e < c ? sh.list[r][e] : kKeyMax;
-        if (lane == 0 && sh.kth[r] != kKeyMax) atomicMin(&kth_shared[pos], static_cast<unsigned long long>(sh.kth[r]));
+        for (int e = lane; e < k; e += 32) out[e] = e < c ? sh.L.list[r][e] : kKeyMax;
+        if (lane == 0 && sh.L.kth[r] != kKeyMax) atomicMin(&kth_shared[pos], static_cast<unsigned long long>(sh.L.kth[r]));
     }
 }
 
@@ -788,7 +683,7 @@ void launch_merge(const uint64_t* seed_keys, const uint64_t* partial, const unsi
 }  // namespace
 
 bool fast_path_supported(int64_t n, int d, int k) {
-    return d >= 1 && d <= kMaxDP && k >= 1 && k <= kMaxK && n >= 2 && static_cast<int64_t>(k) < n &&
+    return d >= 1 && d <= kMaxWideD && k >= 1 && k <= kMaxK && n >= 2 && static_cast<int64_t>(k) < n &&
            n <= (static_cast<int64_t>(1) << 30);
 }
 
@@ -796,6 +691,7 @@ bool fast_path_supported(int64_t n, int d, int k) {
 void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int k, int32_t* nbr_idx, float* nbr_d2,
                       float* kdist2) {
     cudaStream_t s = stream_;
+    const bool wide = d > kMaxDP;
     const int dp = d <= 2 ? 2 : d <= 4 ? 4 : d <= 6 ? 6 : 8;
     const int nt = static_cast<int>(ceil_div(n, kCT));
     const int64_t padded = static_cast<int64_t>(nt) * kCT;
@@ -804,14 +700,17 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
     const int nsplit = nt > 1 ? choose_splits(nt, sms) : 1;
 
     // 1. Morton keys of the centred coordinates, then a stable radix sort.
-    unsigned* mm = reinterpret_cast<unsigned*>(sort_hist_.get(2 * sizeof(unsigned) * d));
+    unsigned* mm = reinterpret_cast<unsigned*>(sort_hist_.get(2 * sizeof(unsigned) * d + sizeof(int) * kMortonDims));
+    int* dims = reinterpret_cast<int*>(mm + 2 * d);
     unsigned* keys = morton_.as<unsigned>(2 * static_cast<size_t>(n));
     unsigned* vals = perm_.as<unsigned>(2 * static_cast<size_t>(n));
     minmax_init_kernel<<<1, 32, 0, s>>>(mm, d);
     CG_LAUNCH_CHECK();
     minmax_kernel<<<grid_for(n, 256), 256, 0, s>>>(xc, n, d, mm);
     CG_LAUNCH_CHECK();
-    morton_kernel<<<grid_for(n, 256), 256, 0, s>>>(xc, n, d, mm, keys, vals);
+    select_dims_kernel<<<1, 32, 0, s>>>(mm, d, dims);
+    CG_LAUNCH_CHECK();
+    morton_kernel<<<grid_for(n, 256), 256, 0, s>>>(xc, n, d, mm, dims, keys, vals);
     CG_LAUNCH_CHECK();
     const int nblocks = static_cast<int>(ceil_div(n, kSortTile));
     unsigned* counts = sort_tmp_.as<unsigned>(static_cast<size_t>(256) * nblocks);
@@ -835,19 +734,22 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
 
     // 2. column tiles
     float* tiles = nullptr;
-    switch (dp) {
+    if (wide) {
+        tiles = cols_.as<float>(wide_tiles_floats(d, nt));
+        wide_build_tiles(xc, norms, n, d, perm, nt, tiles, s);
+    } else switch (dp) {
         case 2: tiles = cols_.as<float>(static_cast<size_t>(tile_floats(2)) * nt); break;
         case 4: tiles = cols_.as<float>(static_cast<size_t>(tile_floats(4)) * nt); break;
         case 6: tiles = cols_.as<float>(static_cast<size_t>(tile_floats(6)) * nt); break;
         default: tiles = cols_.as<float>(static_cast<size_t>(tile_floats(8)) * nt); break;
     }
-    switch (dp) {
+    if (!wide) switch (dp) {
         case 2: build_tiles_kernel<2><<<grid_for(padded, 256), 256, 0, s>>>(xc, norms, n, d, perm, padded, tiles); break;
         case 4: build_tiles_kernel<4><<<grid_for(padded, 256), 256, 0, s>>>(xc, norms, n, d, perm, padded, tiles); break;
         case 6: build_tiles_kernel<6><<<grid_for(padded, 256), 256, 0, s>>>(xc, norms, n, d, perm, padded, tiles); break;
         default: build_tiles_kernel<8><<<grid_for(padded, 256), 256, 0, s>>>(xc, norms, n, d, perm, padded, tiles); break;
     }
-    CG_LAUNCH_CHECK();
+    if (!wide) CG_LAUNCH_CHECK();
 
     // 3. seed lists and the shared k-th keys
     char* rows = static_cast<char*>(rows_.get(padded * sizeof(uint64_t) * (k + 1) +
@@ -858,17 +760,20 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
     int* status = status_ptr();
     const unsigned* maxn = reinterpret_cast<const unsigned*>(max_norm_.get(sizeof(unsigned)));
     mark(2);
-    switch (dp) {
+    if (wide) wide_seed(tiles, nt, d, k, seed_keys, kth_shared, s);
+    else switch (dp) {
         case 2: seed_kernel<2><<<nt, kThreads, 0, s>>>(tiles, nt, n, k, seed_keys, kth_shared); break;
         case 4: seed_kernel<4><<<nt, kThreads, 0, s>>>(tiles, nt, n, k, seed_keys, kth_shared); break;
         case 6: seed_kernel<6><<<nt, kThreads, 0, s>>>(tiles, nt, n, k, seed_keys, kth_shared); break;
         default: seed_kernel<8><<<nt, kThreads, 0, s>>>(tiles, nt, n, k, seed_keys, kth_shared); break;
     }
-    CG_LAUNCH_CHECK();
+    if (!wide) CG_LAUNCH_CHECK();
     mark(3);
 
     // 4. sweep over the other tiles, split S ways
-    if (nt > 1) {
+    if (nt > 1 && wide) {
+        wide_sweep(tiles, nt, nsplit, d, k, maxn, kth_shared, partial, s);
+    } else if (nt > 1) {
         const bool big = k > 32;
 #define CG_SWEEP(DPV)                                                                                 \
     (big ? launch_sweep<DPV, 96>(tiles, nt, nsplit, k, maxn, kth_shared, partial, status, s)          \

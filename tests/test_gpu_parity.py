@@ -73,6 +73,10 @@ KNN_CASES = [
     ("k64", lambda: synthetic.clusters_with_outliers(5000, 8, seed=23), 64),
     ("k33_d3", lambda: synthetic.clusters_with_outliers(3000, 3, seed=24), 33),
     ("d1", lambda: synthetic.clusters_with_outliers(2000, 1, seed=25), 10),
+    # the wide-point sweep: d not a multiple of 16, d = 128 with k = 50
+    ("d9", lambda: synthetic.clusters_with_outliers(3000, 9, seed=26), 20),
+    ("d100_k40", lambda: synthetic.reference_test_data(2500, 100, seed=27, n_outliers=25), 40),
+    ("factor_d128_k50", lambda: synthetic.factor_model(3000, 128, seed=28), 50),
     # 10,000 points on 50 positions: every point has 199 exact duplicates,
     # which drives list overflows and the exact re-run of a block
     ("dups_heavy", lambda: np.repeat(np.random.default_rng(5).uniform(-3, 3, (50, 4)).astype(np.float32), 200,
@@ -100,6 +104,8 @@ def test_auto_selects_the_fast_path_for_small_d(ctx):
     ctx.lof(synthetic.reference_test_data(600, 4, seed=5), 257)
     assert ctx.last_path() == _culof.PATH_GENERAL
     ctx.lof(synthetic.reference_test_data(600, 32, seed=5), 20)
+    assert ctx.last_path() == _culof.PATH_FAST
+    ctx.lof(synthetic.reference_test_data(600, 200, seed=5), 20)
     assert ctx.last_path() == _culof.PATH_GENERAL
 
 
