@@ -60,6 +60,9 @@ def parse_args():
     p.add_argument("--cpu-seconds", type=float, default=8.0, help="target CPU time of the baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--path", choices=["auto", "fast", "general"], default="auto")
+    p.add_argument("--workload", choices=["clusters", "factor", "mixture"], default="clusters",
+                   help="clusters: 5 clusters + 1%% outliers; factor: rank-16 factor model + 5.0 shift + 0.5%% noisy "
+                        "rows; mixture: 8 clusters + 1%% outliers")
     return p.parse_args()
 
 
@@ -73,7 +76,18 @@ def dist_env():
 def workload(args):
     from culof_gb300 import synthetic
 
+    if args.workload == "factor":
+        return synthetic.factor_model(args.n, args.d, seed=args.seed)
+    if args.workload == "mixture":
+        return synthetic.gradient_mixture(args.n, args.d, seed=args.seed)
     return synthetic.clusters_with_outliers(args.n, args.d, seed=args.seed)
+
+
+GENERATORS = {
+    "clusters": "5 isotropic Gaussian clusters (centres U[-10,10]^d, sigma U[0.5,2]) + 1% U[-15,15]^d",
+    "factor": "rank-16 Gaussian factor model (loadings N(0,1/16)) + N(0,0.1^2) noise + 5.0 shift, 0.5% rows + U[-3,3]^d",
+    "mixture": "8 Gaussian clusters (centres U[-8,8]^d, sigma U[0.5,1.5]) + 1% U[-12,12]^d",
+}
 
 
 def config_dict(args, extra=None):
@@ -83,8 +97,7 @@ def config_dict(args, extra=None):
         "d": args.d,
         "k": args.k,
         "contamination": args.contamination,
-        "generator": "5 isotropic Gaussian clusters (centres U[-10,10]^d, sigma U[0.5,2]) + 1% U[-15,15]^d, seed "
-        + str(args.seed),
+        "generator": GENERATORS[args.workload] + ", seed " + str(args.seed),
         "l2": "256 MiB write between timed steps, outside the events (X is 6.4 MB < L2)",
         "parallelism": "replicas" if int(os.environ.get("WORLD_SIZE", "1")) > 1 else "single GPU",
     }
