@@ -362,6 +362,7 @@ struct SweepSmem {
     RowLists<M> L;
     uint64_t full_bar[kStages];
     float rowc[kRT][DP];
+    uint64_t rowd[kRT][DP];  // (-2a, -2a) per row and dimension: the packed FMA operands
     int done[kStages];
     uint16_t queue[kWarps][kQueueCap];
 };
@@ -431,7 +432,10 @@ sweep_kernel(const float* __restrict__ tiles, int nt, int nsplit, int k, const u
                           : tau_from(kk, nr, nmax, DP);
         sh.L.cnt[tid] = 0;
 #pragma unroll
-        for (int f = 0; f < DP; ++f) sh.rowc[tid][f] = tile_coord<DP>(own, tid, f);
+        for (int f = 0; f < DP; ++f) {
+            sh.rowc[tid][f] = tile_coord<DP>(own, tid, f);
+            sh.rowd[tid][f] = dup2(-2.0f * sh.rowc[tid][f]);
+        }
     }
     if (tid < kStages) sh.done[tid] = 0;
     if (tid == 0) {
@@ -455,7 +459,12 @@ sweep_kernel(const float* __restrict__ tiles, int nt, int nsplit, int k, const u
 #pragma unroll
     for (int j = 0; j < kRowsPerLane; ++j) {
 #pragma unroll
-        for (int f = 0; f < DP; ++f) a2[j][f] = dup2(-2.0f * sh.rowc[rbase + j][f]);
+        for (int f = 0; f < DP; ++f) {
+            // Loaded as 64-bit pairs from shared memory: the compiler cannot see
+            // that both halves are equal, so each operand stays a register pair
+            // for the whole sweep (rebuilding the pair costs a move per FMA).
+            a2[j][f] = sh.rowd[rbase + j][f];
+        }
         tau_r[j] = sh.L.tau[rbase + j];
         tau2[j] = dup2(tau_above(tau_r[j]));
     }
@@ -587,57 +596,69 @@ sweep_kernel(const float* __restrict__ tiles, int nt, int nsplit, int k, const u
 // ---------------------------------------------------------------- merge
 
 // Per row (one warp): the k smallest of the seed list and the S split lists,
-// written in the reference's slot order.
-template <int E>
-__global__ void merge_kernel(const uint64_t* __restrict__ seed_keys, const uint64_t* __restrict__ partial,
-                             const unsigned* __restrict__ perm, int64_t n, int nt, int nsplit, int k,
-                             int32_t* __restrict__ nbr_idx, float* __restrict__ nbr_d2, float* __restrict__ kdist2) {
-    const int lane = threadIdx.x & 31;
-    const int64_t pos = static_cast<int64_t>(blockIdx.x) * (blockDim.x >> 5) + (threadIdx.x >> 5);
+// written in the reference's slot order. The lists are sorted, disjoint
+// (different columns) and kKeyMax padded, so an element's final rank is its
+// position in its own list plus, for every other list, the count of keys
+// below it (a binary search in shared memory); no sort is needed. In the
+// result the ties with the k-th key already sit at the end in index order;
+// the keys below it are placed by counting smaller indices among them.
+constexpr int kMergeWarps = 8;
+
+__global__ void __launch_bounds__(32 * kMergeWarps)
+merge_kernel(const uint64_t* __restrict__ seed_keys, const uint64_t* __restrict__ partial,
+             const unsigned* __restrict__ perm, int64_t n, int nt, int nsplit, int k, int32_t* __restrict__ nbr_idx,
+             float* __restrict__ nbr_d2, float* __restrict__ kdist2) {
+    extern __shared__ uint64_t msh[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nl = nsplit + 1, total = nl * k;
+    uint64_t* lists = msh + static_cast<int64_t>(warp) * (total + k);
+    uint64_t* out = lists + total;
+    const int64_t pos = static_cast<int64_t>(blockIdx.x) * kMergeWarps + warp;
     if (pos >= n) return;
-    const int total = (nsplit + 1) * k;
-    uint64_t v[E];
-#pragma unroll
-    for (int j = 0; j < E; ++j) {
-        const int e = j * 32 + lane;
-        uint64_t key = kKeyMax;
-        if (e < k) key = seed_keys[pos * k + e];
-        else if (e < total) {
-            const int s = e / k - 1, t = e % k;
-            key = partial[(static_cast<int64_t>(s) * nt * kRT + pos) * k + t];
+    for (int e = lane; e < total; e += 32) {
+        const int l = e / k, t = e % k;
+        lists[e] = (l == 0) ? seed_keys[pos * k + t]
+                            : partial[(static_cast<int64_t>(l - 1) * nt * kRT + pos) * k + t];
+    }
+    for (int e = lane; e < k; e += 32) out[e] = kKeyMax;
+    __syncwarp();
+    for (int e = lane; e < total; e += 32) {
+        const uint64_t x = lists[e];
+        if (x == kKeyMax) continue;
+        const int l = e / k;
+        int rank = e % k;
+        for (int o = 0; o < nl && rank < k; ++o) {
+            if (o == l) continue;
+            const uint64_t* lo = lists + o * k;
+            int a = 0, b = k;  // count of keys < x in list o
+            while (a < b) {
+                const int mid = (a + b) >> 1;
+                if (lo[mid] < x) a = mid + 1;
+                else b = mid;
+            }
+            rank += a;
         }
-        v[j] = key;
+        if (rank < k) out[rank] = x;
     }
-    warp_bitonic_sort<E>(v);
-    // k-th key
-    const int owner = (k - 1) & 31, oreg = (k - 1) >> 5;
-    uint64_t kth = kKeyMax;
-#pragma unroll
-    for (int j = 0; j < E; ++j) {
-        const uint64_t t = __shfl_sync(0xffffffffu, v[j], owner);
-        if (j == oreg) kth = t;
-    }
+    __syncwarp();
+    const uint64_t kth = out[k - 1];
     const uint32_t kbits = key_bits(kth);
-    // re-key the first k: (tie << 63) | (index << 32) | bits; others max
+    // keys strictly below the k-th occupy out[0, below); the ties follow
+    int below = 0;
+    for (int e = lane; e < k; e += 32) below += key_bits(out[e]) < kbits ? 1 : 0;
 #pragma unroll
-    for (int j = 0; j < E; ++j) {
-        const int e = j * 32 + lane;
-        if (e < k) {
-            const uint32_t b = key_bits(v[j]);
-            v[j] = (static_cast<uint64_t>(b == kbits) << 63) | (static_cast<uint64_t>(key_index(v[j])) << 32) | b;
-        } else {
-            v[j] = kKeyMax;
-        }
-    }
-    warp_bitonic_sort<E>(v);
+    for (int o = 16; o > 0; o >>= 1) below += __shfl_xor_sync(0xffffffffu, below, o);
     const unsigned self = perm[pos];
-#pragma unroll
-    for (int j = 0; j < E; ++j) {
-        const int e = j * 32 + lane;
-        if (e < k) {
-            nbr_idx[static_cast<int64_t>(e) * n + self] = static_cast<int32_t>((v[j] >> 32) & 0x7FFFFFFFull);
-            nbr_d2[static_cast<int64_t>(e) * n + self] = __uint_as_float(static_cast<uint32_t>(v[j]));
+    for (int e = lane; e < k; e += 32) {
+        const uint64_t y = out[e];
+        int slot = e;  // ties: already in index order after the keys below
+        if (e < below) {
+            const uint32_t yi = key_index(y);
+            slot = 0;
+            for (int q = 0; q < below; ++q) slot += key_index(out[q]) < yi ? 1 : 0;
         }
+        nbr_idx[static_cast<int64_t>(slot) * n + self] = static_cast<int32_t>(key_index(y) & 0x7FFFFFFFu);
+        nbr_d2[static_cast<int64_t>(slot) * n + self] = __uint_as_float(key_bits(y));
     }
     if (lane == 0) kdist2[self] = __uint_as_float(kbits);
 }
@@ -671,11 +692,12 @@ void launch_sweep(const float* tiles, int nt, int nsplit, int k, const unsigned*
     CG_LAUNCH_CHECK();
 }
 
-template <int E>
 void launch_merge(const uint64_t* seed_keys, const uint64_t* partial, const unsigned* perm, int64_t n, int nt,
                   int nsplit, int k, int32_t* idx, float* d2, float* kd, cudaStream_t s) {
-    const int rows_per_block = 8;
-    merge_kernel<E><<<static_cast<unsigned>(ceil_div(n, rows_per_block)), 32 * rows_per_block, 0, s>>>(
+    const size_t smem = sizeof(uint64_t) * kMergeWarps * static_cast<size_t>((nsplit + 1) * k + k);
+    if (smem > 48 * 1024)
+        CG_CUDA(cudaFuncSetAttribute(merge_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+    merge_kernel<<<static_cast<unsigned>(ceil_div(n, kMergeWarps)), 32 * kMergeWarps, smem, s>>>(
         seed_keys, partial, perm, n, nt, nsplit, k, idx, d2, kd);
     CG_LAUNCH_CHECK();
 }
@@ -790,11 +812,7 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
     mark(4);
 
     // 5. merge into the reference slot order
-    const int total = (ns + 1) * k;
-    if (total <= 64) launch_merge<2>(seed_keys, partial, perm, n, nt, ns, k, nbr_idx, nbr_d2, kdist2, s);
-    else if (total <= 128) launch_merge<4>(seed_keys, partial, perm, n, nt, ns, k, nbr_idx, nbr_d2, kdist2, s);
-    else if (total <= 256) launch_merge<8>(seed_keys, partial, perm, n, nt, ns, k, nbr_idx, nbr_d2, kdist2, s);
-    else launch_merge<16>(seed_keys, partial, perm, n, nt, ns, k, nbr_idx, nbr_d2, kdist2, s);
+    launch_merge(seed_keys, partial, perm, n, nt, ns, k, nbr_idx, nbr_d2, kdist2, s);
 }
 
 }  // namespace culof_gb300
