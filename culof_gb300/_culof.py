@@ -78,6 +78,7 @@ _SIGS = {
     "culof_compute_scores": ([_P, _P, _P, _I64, _I, _P], _I),
     "culof_context_contamination_offset_device": ([_P, _P, _I64, _D, _P], _I),
     "culof_contamination_offset_noalloc": ([_P, _P, _I64, _D, _P], _I),
+    "culof_context_bf16_gram": ([_P, _P, _I64, _P, _I64, _I, _P], _I),
 }
 for _name, (_args, _res) in _SIGS.items():
     _fn = getattr(_lib, _name)
@@ -276,6 +277,10 @@ class Context:
                    kdist2: int) -> None:
         _check(_lib.culof_context_knn_device(self._h, points, n, d, int(k), int(bool(normalize)), nbr_idx, nbr_d2,
                                              kdist2))
+
+    def bf16_gram(self, A: int, rows_a: int, B: int, rows_b: int, K: int, G: int) -> None:
+        """G = A B^T on the tensor cores (bf16 in, f32 out; device pointers)."""
+        _check(_lib.culof_context_bf16_gram(self._h, A, rows_a, B, rows_b, K, G))
 
     def offset_device(self, nof: int, n: int, contamination, offset: int) -> None:
         c = -1.0 if contamination == "auto" else float(contamination)

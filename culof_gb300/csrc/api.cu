@@ -248,6 +248,14 @@ int culof_compute_scores(void* cuda_stream, const int32_t* d_nbr_idx, const floa
     });
 }
 
+int culof_context_bf16_gram(culof_context* ctx, const void* d_A, int64_t rows_a, const void* d_B, int64_t rows_b,
+                            int K, float* d_G) {
+    return guarded([&] {
+        if (!d_A || !d_B || !d_G) throw Error(culof_gb300::kInvalidArgument, "device pointers must not be null");
+        engine_of(ctx).bf16_gram(d_A, rows_a, d_B, rows_b, K, d_G);
+    });
+}
+
 int culof_context_contamination_offset_device(culof_context* ctx, const float* d_nof, int64_t n_points,
                                               double contamination, double* d_offset) {
     return guarded([&] {

@@ -8,6 +8,7 @@
 
 #include "engine.cuh"
 #include "fast.cuh"
+#include "tc_host.cuh"
 
 namespace culof_gb300 {
 
@@ -169,6 +170,11 @@ void Engine::offset_device(const float* d_nof, int64_t n, double contamination, 
     validate_contamination(contamination);
     void* scratch = offset_scratch_.get(offset_scratch_bytes());
     contamination_offset(d_nof, n, plan_offset(n, contamination), scratch, d_offset, stream_);
+}
+
+void Engine::bf16_gram(const void* A, int64_t rows_a, const void* B, int64_t rows_b, int K, float* G) {
+    CG_CUDA(cudaSetDevice(device_));
+    tc::bf16_gram(A, rows_a, B, rows_b, K, G, status_ptr(), stream_);
 }
 
 void Engine::fit_predict_device(const float* d_x, int64_t n, int d, int k, bool normalize,

@@ -55,6 +55,7 @@ public:
     void fit_predict_device(const float* d_x, int64_t n, int d, int k, bool normalize,
                             double contamination, float* d_nof, int64_t* d_labels, double* d_offset);
     void offset_device(const float* d_nof, int64_t n, double contamination, double* d_offset);
+    void bf16_gram(const void* A, int64_t rows_a, const void* B, int64_t rows_b, int K, float* G);
 
     // Host-pointer forms: copy in, run, copy out, synchronise.
     void lof_host(const float* x, int64_t n, int d, int k, bool normalize, float* scores);

@@ -472,7 +472,7 @@ sweep_kernel(const float* __restrict__ tiles, int nt, int nsplit, int k, const u
     bool ok = true;
     for (int m = 0; m < count && ok; ++m) {
         const int stage = m % kStages;
-        if (!mbar_wait(&sh.full_bar[stage], (m / kStages) & 1)) {
+        if (!mbar_wait_warp(&sh.full_bar[stage], (m / kStages) & 1)) {
             ok = false;
             break;
         }

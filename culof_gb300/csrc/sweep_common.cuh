@@ -91,6 +91,16 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
     }
     return false;
 }
+// Warp-uniform bounded wait: every lane polls, and the warp leaves the loop
+// together (all lanes saw the phase complete, or all gave up), so no lane
+// can run ahead into warp-synchronous code alone.
+__device__ __forceinline__ bool mbar_wait_warp(uint64_t* bar, unsigned parity) {
+    for (long long it = 0; it < kSpinLimit; ++it) {
+        if (__all_sync(0xffffffffu, mbar_try_wait(bar, parity))) return true;
+        if (it > 64) __nanosleep(64);
+    }
+    return false;
+}
 __device__ __forceinline__ void tma_load_1d(void* smem_dst, const void* gmem_src, unsigned bytes, uint64_t* bar) {
     asm volatile(
         "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(

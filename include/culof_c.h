@@ -148,6 +148,15 @@ CULOF_API int culof_compute_lrd(void* cuda_stream, const int32_t* d_nbr_idx, con
 CULOF_API int culof_compute_scores(void* cuda_stream, const int32_t* d_nbr_idx, const float* d_lrd,
                          int64_t n_points, int k, float* d_scores);
 
+/* The tensor-core building block of the precision form: G = A B^T for
+ * row-major bf16 operands A (rows_a x K) and B (rows_b x K), f32 accumulation
+ * (tcgen05.mma, TMEM). rows_a and rows_b multiples of 128, K = 128; device
+ * pointers 16-byte aligned; G row-major (rows_a x rows_b). Asynchronous on the
+ * context stream; errors surface at culof_context_synchronize. No reference
+ * counterpart (the reference's Gram tile is cuBLAS SGEMM, pipeline.cu:182-188). */
+CULOF_API int culof_context_bf16_gram(culof_context* ctx, const void* d_A, int64_t rows_a, const void* d_B,
+                                      int64_t rows_b, int K, float* d_G);
+
 /* src/culof/__init__.py:179-185 offset_: np.percentile(d_nof, 100 * contamination)
  * computed on the GPU (contamination <= 0: 'auto', -1.5). d_offset: device double. */
 CULOF_API int culof_context_contamination_offset_device(culof_context* ctx, const float* d_nof,
