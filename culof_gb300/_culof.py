@@ -29,7 +29,7 @@ ERR_NO_DEVICE = 3
 ERR_INTERNAL = 4
 ERR_KERNEL = 5
 
-PATH_AUTO, PATH_FAST, PATH_GENERAL = 0, 1, 2
+PATH_AUTO, PATH_FAST, PATH_GENERAL, PATH_TENSOR = 0, 1, 2, 3
 
 
 class CudaError(RuntimeError):

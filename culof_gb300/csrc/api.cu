@@ -126,7 +126,7 @@ int culof_context_synchronize(culof_context* ctx) {
 
 int culof_context_set_path(culof_context* ctx, int path) {
     return guarded([&] {
-        if (path < CULOF_PATH_AUTO || path > CULOF_PATH_GENERAL)
+        if (path < CULOF_PATH_AUTO || path > CULOF_PATH_TENSOR)
             throw Error(culof_gb300::kInvalidArgument, "unknown path");
         engine_of(ctx).set_path(path);
     });

@@ -97,18 +97,26 @@ int Engine::tile_rows_for(int64_t n) {
     return choose_tile_rows(n, usable < cap ? usable : cap);
 }
 
-bool Engine::use_fast_path(int64_t n, int d, int k) const {
+// AUTO: the FP32 fused sweep for d <= 8, the tensor-core sweep for
+// 8 < d <= 128, the general tile + select path beyond the fused paths'
+// limits (d > 128 or k > 64). CULOF_GB300_PATH=general|fast|tensor overrides
+// AUTO for a process.
+int Engine::choose_path(int64_t n, int d, int k) const {
     int p = path_;
     if (p == kPathAuto) {
         if (const char* env = std::getenv("CULOF_GB300_PATH")) {
             if (env[0] == 'g') p = kPathGeneral;
             if (env[0] == 'f') p = kPathFast;
+            if (env[0] == 't') p = kPathTensor;
         }
     }
     const bool ok = fast_path_supported(n, d, k);
-    if (p == kPathGeneral) return false;
-    if (p == kPathFast && !ok) throw Error(kInvalidArgument, "fast path requested but unsupported for this n/d/k");
-    return ok;
+    if (p == kPathGeneral) return kPathGeneral;
+    if ((p == kPathFast || p == kPathTensor) && !ok)
+        throw Error(kInvalidArgument, "fused path requested but unsupported for this n/d/k");
+    if (p == kPathFast || p == kPathTensor) return p;
+    if (!ok) return kPathGeneral;
+    return d > 8 ? kPathTensor : kPathFast;
 }
 
 void Engine::knn_general(const float* xc, const float* norms, int64_t n, int d, int k,
@@ -137,10 +145,11 @@ void Engine::knn(const float* d_x, int64_t n, int d, int k, bool normalize, int3
     mark(0);
     center(d_x, n, d, normalize, xc, partial, mean, inv, stream_);
     squared_norms(xc, n, d, norms, maxn, stream_);
-    if (use_fast_path(n, d, k)) {
-        last_path_ = kPathFast;
+    const int path = choose_path(n, d, k);
+    if (path != kPathGeneral) {
+        last_path_ = path;
         mark(1);
-        knn_fast(xc, norms, n, d, k, nbr_idx, nbr_d2, kdist2);
+        knn_fast(xc, norms, n, d, k, path == kPathTensor, nbr_idx, nbr_d2, kdist2);
     } else {
         last_path_ = kPathGeneral;
         mark(1);

@@ -30,7 +30,7 @@ private:
     size_t cap_ = 0;
 };
 
-enum Path : int { kPathAuto = 0, kPathFast = 1, kPathGeneral = 2 };
+enum Path : int { kPathAuto = 0, kPathFast = 1, kPathGeneral = 2, kPathTensor = 3 };
 
 class Engine {
 public:
@@ -63,10 +63,10 @@ public:
                           double contamination, float* nof, int64_t* labels, double* offset);
 
 private:
-    bool use_fast_path(int64_t n, int d, int k) const;
+    int choose_path(int64_t n, int d, int k) const;
     void knn_general(const float* xc, const float* norms, int64_t n, int d, int k, int32_t* nbr_idx,
                      float* nbr_d2, float* kdist2);
-    void knn_fast(const float* xc, const float* norms, int64_t n, int d, int k, int32_t* nbr_idx,
+    void knn_fast(const float* xc, const float* norms, int64_t n, int d, int k, bool tensor, int32_t* nbr_idx,
                   float* nbr_d2, float* kdist2);
     int tile_rows_for(int64_t n);
 

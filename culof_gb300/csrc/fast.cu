@@ -669,6 +669,8 @@ int grid_for(int64_t items, int block) {
     return static_cast<int>(g < 1 ? 1 : g);
 }
 
+}  // namespace
+
 int choose_splits(int nt, int sms) {
     // enough CTAs (2 per SM resident) for ~16 waves, at most 7 splits
     const int want = (32 * sms + nt - 1) / nt;
@@ -677,6 +679,8 @@ int choose_splits(int nt, int sms) {
     if (s > nt - 1) s = nt - 1 > 0 ? nt - 1 : 1;
     return s;
 }
+
+namespace {
 
 template <int DP, int M>
 void launch_sweep(const float* tiles, int nt, int nsplit, int k, const unsigned* maxn, unsigned long long* kth_shared,
@@ -692,6 +696,8 @@ void launch_sweep(const float* tiles, int nt, int nsplit, int k, const unsigned*
     CG_LAUNCH_CHECK();
 }
 
+}  // namespace
+
 void launch_merge(const uint64_t* seed_keys, const uint64_t* partial, const unsigned* perm, int64_t n, int nt,
                   int nsplit, int k, int32_t* idx, float* d2, float* kd, cudaStream_t s) {
     const size_t smem = sizeof(uint64_t) * kMergeWarps * static_cast<size_t>((nsplit + 1) * k + k);
@@ -702,18 +708,16 @@ void launch_merge(const uint64_t* seed_keys, const uint64_t* partial, const unsi
     CG_LAUNCH_CHECK();
 }
 
-}  // namespace
-
 bool fast_path_supported(int64_t n, int d, int k) {
     return d >= 1 && d <= kMaxWideD && k >= 1 && k <= kMaxK && n >= 2 && static_cast<int64_t>(k) < n &&
            n <= (static_cast<int64_t>(1) << 30);
 }
 
 // Host orchestration of the fast path.
-void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int k, int32_t* nbr_idx, float* nbr_d2,
-                      float* kdist2) {
+void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int k, bool tensor, int32_t* nbr_idx,
+                      float* nbr_d2, float* kdist2) {
     cudaStream_t s = stream_;
-    const bool wide = d > kMaxDP;
+    const bool wide = !tensor && d > kMaxDP;
     const int dp = d <= 2 ? 2 : d <= 4 ? 4 : d <= 6 ? 6 : 8;
     const int nt = static_cast<int>(ceil_div(n, kCT));
     const int64_t padded = static_cast<int64_t>(nt) * kCT;
@@ -756,7 +760,10 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
 
     // 2. column tiles
     float* tiles = nullptr;
-    if (wide) {
+    TcBuffers tcb{};
+    if (tensor) {
+        tcb = tc_prepare(cols_.get(tc_buffer_bytes(padded, d)), xc, norms, n, d, perm, nt, mm, s);
+    } else if (wide) {
         tiles = cols_.as<float>(wide_tiles_floats(d, nt));
         wide_build_tiles(xc, norms, n, d, perm, nt, tiles, s);
     } else switch (dp) {
@@ -765,13 +772,13 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
         case 6: tiles = cols_.as<float>(static_cast<size_t>(tile_floats(6)) * nt); break;
         default: tiles = cols_.as<float>(static_cast<size_t>(tile_floats(8)) * nt); break;
     }
-    if (!wide) switch (dp) {
+    if (!wide && !tensor) switch (dp) {
         case 2: build_tiles_kernel<2><<<grid_for(padded, 256), 256, 0, s>>>(xc, norms, n, d, perm, padded, tiles); break;
         case 4: build_tiles_kernel<4><<<grid_for(padded, 256), 256, 0, s>>>(xc, norms, n, d, perm, padded, tiles); break;
         case 6: build_tiles_kernel<6><<<grid_for(padded, 256), 256, 0, s>>>(xc, norms, n, d, perm, padded, tiles); break;
         default: build_tiles_kernel<8><<<grid_for(padded, 256), 256, 0, s>>>(xc, norms, n, d, perm, padded, tiles); break;
     }
-    if (!wide) CG_LAUNCH_CHECK();
+    if (!wide && !tensor) CG_LAUNCH_CHECK();
 
     // 3. seed lists and the shared k-th keys
     char* rows = static_cast<char*>(rows_.get(padded * sizeof(uint64_t) * (k + 1) +
@@ -782,18 +789,21 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
     int* status = status_ptr();
     const unsigned* maxn = reinterpret_cast<const unsigned*>(max_norm_.get(sizeof(unsigned)));
     mark(2);
-    if (wide) wide_seed(tiles, nt, d, k, seed_keys, kth_shared, s);
+    if (tensor) tc_seed(tcb, nt, d, k, seed_keys, kth_shared, s);
+    else if (wide) wide_seed(tiles, nt, d, k, seed_keys, kth_shared, s);
     else switch (dp) {
         case 2: seed_kernel<2><<<nt, kThreads, 0, s>>>(tiles, nt, n, k, seed_keys, kth_shared); break;
         case 4: seed_kernel<4><<<nt, kThreads, 0, s>>>(tiles, nt, n, k, seed_keys, kth_shared); break;
         case 6: seed_kernel<6><<<nt, kThreads, 0, s>>>(tiles, nt, n, k, seed_keys, kth_shared); break;
         default: seed_kernel<8><<<nt, kThreads, 0, s>>>(tiles, nt, n, k, seed_keys, kth_shared); break;
     }
-    if (!wide) CG_LAUNCH_CHECK();
+    if (!wide && !tensor) CG_LAUNCH_CHECK();
     mark(3);
 
     // 4. sweep over the other tiles, split S ways
-    if (nt > 1 && wide) {
+    if (nt > 1 && tensor) {
+        tc_sweep(tcb, nt, nsplit, d, k, maxn, kth_shared, partial, status, s);
+    } else if (nt > 1 && wide) {
         wide_sweep(tiles, nt, nsplit, d, k, maxn, kth_shared, partial, s);
     } else if (nt > 1) {
         const bool big = k > 32;

@@ -20,4 +20,30 @@ void wide_seed(const float* tiles, int nt, int d, int k, uint64_t* seed_keys, un
 void wide_sweep(const float* tiles, int nt, int nsplit, int d, int k, const unsigned* maxn,
                 unsigned long long* kth_shared, uint64_t* partial, cudaStream_t s);
 
+// Shared by the FP32 and tensor-core sweeps (fast.cu).
+int choose_splits(int nt, int sms);
+void launch_merge(const uint64_t* seed_keys, const uint64_t* partial, const unsigned* perm, int64_t n, int nt,
+                  int nsplit, int k, int32_t* idx, float* d2, float* kd, cudaStream_t s);
+
+// The tensor-core variant (tc_sweep.cu). Sorted-order arrays of one call:
+// xh f16 operand rows [padded][Kp], xr FP32 coordinates [padded][dr], cn
+// norms, ix original indices, scale a device record of the f16 scaling.
+struct TcBuffers {
+    void* xh;
+    float* xr;
+    float* cn;
+    unsigned* ix;
+    void* scale;
+    int Kp;
+    int dr;
+};
+size_t tc_buffer_bytes(int64_t padded, int d);
+// minmax: the per-dimension (min, max) keys of the spatial-order pass.
+TcBuffers tc_prepare(void* buf, const float* xc, const float* norms, int64_t n, int d, const unsigned* perm, int nt,
+                     const unsigned* minmax, cudaStream_t s);
+void tc_seed(const TcBuffers& b, int nt, int d, int k, uint64_t* seed_keys, unsigned long long* kth_shared,
+             cudaStream_t s);
+void tc_sweep(const TcBuffers& b, int nt, int nsplit, int d, int k, const unsigned* maxn,
+              unsigned long long* kth_shared, uint64_t* partial, int* status, cudaStream_t s);
+
 }  // namespace culof_gb300

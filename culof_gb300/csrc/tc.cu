@@ -35,7 +35,7 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
 
 }  // namespace
 
-CUtensorMap make_kmajor_bf16_map(const void* base, int64_t rows, int K) {
+CUtensorMap make_kmajor_map(const void* base, int64_t rows, int K, bool fp16) {
     if (K % 64 != 0) throw Error(kInvalidArgument, "K must be a multiple of 64");
     if (reinterpret_cast<uintptr_t>(base) % 16 != 0) throw Error(kInvalidArgument, "operand base must be 16-byte aligned");
     CUtensorMap map;
@@ -43,7 +43,7 @@ CUtensorMap make_kmajor_bf16_map(const void* base, int64_t rows, int K) {
     const cuuint64_t strides[1] = {static_cast<cuuint64_t>(K) * 2};
     const cuuint32_t box[2] = {64, 128};
     const cuuint32_t estr[2] = {1, 1};
-    const CUresult r = encode_fn()(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides,
+    const CUresult r = encode_fn()(&map, fp16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides,
                                    box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                                    CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) throw Error(kCudaError, "cuTensorMapEncodeTiled failed");

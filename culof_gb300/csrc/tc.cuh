@@ -11,10 +11,21 @@
 namespace culof_gb300 {
 namespace tc {
 
-// A 2-D bf16 tensor map over a row-major [rows][K] array (K contiguous),
-// loaded in boxes of 64 K-elements x 128 rows with 128-byte swizzle, the
-// canonical K-major operand layout of tcgen05.mma. K must be a multiple of 64.
-CUtensorMap make_kmajor_bf16_map(const void* base, int64_t rows, int K);
+// A 2-D 16-bit (bf16 or f16) tensor map over a row-major [rows][K] array
+// (K contiguous), loaded in boxes of 64 K-elements x 128 rows with 128-byte
+// swizzle, the canonical K-major operand layout of tcgen05.mma. K must be a
+// multiple of 64.
+CUtensorMap make_kmajor_map(const void* base, int64_t rows, int K, bool fp16);
+inline CUtensorMap make_kmajor_bf16_map(const void* base, int64_t rows, int K) {
+    return make_kmajor_map(base, rows, K, false);
+}
+
+// Instruction descriptor of tcgen05.mma kind::f16: f16 x f16 -> f32,
+// both operands K-major, shape M x N.
+__host__ __device__ constexpr uint32_t f16_idesc(int M, int N) {
+    return (1u << 4)  // D: f32 (A, B: f16 = 0)
+           | (static_cast<uint32_t>(N >> 3) << 17) | (static_cast<uint32_t>(M >> 4) << 24);
+}
 
 // ---- device helpers ------------------------------------------------------
 using sweep::smem_u32;

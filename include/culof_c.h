@@ -37,9 +37,10 @@ extern "C" {
 #define CULOF_ERR_KERNEL 5 /* a kernel reported an error status word (e.g. a bounded wait expired) */
 
 /* Path selection for culof_context_set_path. */
-#define CULOF_PATH_AUTO 0
-#define CULOF_PATH_FAST 1    /* fused distance + filtered select (small d, k <= 64)  */
-#define CULOF_PATH_GENERAL 2 /* exact distance tile + radix select (any d, any k)    */
+#define CULOF_PATH_AUTO 0    /* FAST for d <= 8, TENSOR for 8 < d <= 128, else GENERAL */
+#define CULOF_PATH_FAST 1    /* fused FP32 distance + filtered select (d <= 128, k <= 64) */
+#define CULOF_PATH_GENERAL 2 /* exact distance tile + radix select (any d, any k)        */
+#define CULOF_PATH_TENSOR 3  /* f16 tensor-core filter + exact rescoring (d <= 128, k <= 64) */
 
 typedef struct culof_context culof_context;
 
@@ -67,7 +68,7 @@ CULOF_API int culof_context_set_stream(culof_context* ctx, void* cuda_stream);
 CULOF_API int culof_context_synchronize(culof_context* ctx);
 /* CULOF_PATH_* (default AUTO). Every path returns bit-identical results. */
 CULOF_API int culof_context_set_path(culof_context* ctx, int path);
-/* Path used by the last k-NN run of this context (CULOF_PATH_FAST/GENERAL). */
+/* Path used by the last k-NN run of this context (CULOF_PATH_FAST/GENERAL/TENSOR). */
 CULOF_API int culof_context_last_path(culof_context* ctx);
 
 /* include/culof.h:46-47 culof::lof(points, n, d, k, normalize).

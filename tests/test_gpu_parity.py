@@ -18,6 +18,8 @@ from culof_gb300 import _culof, synthetic
 pytestmark = pytest.mark.gpu
 
 PATHS = [_culof.PATH_AUTO, _culof.PATH_GENERAL]
+# every k-NN case also runs through each forced fused path that supports it
+KNN_PATHS = [_culof.PATH_AUTO, _culof.PATH_GENERAL, _culof.PATH_FAST, _culof.PATH_TENSOR]
 
 
 def torch_cuda():
@@ -84,10 +86,12 @@ KNN_CASES = [
 ]
 
 
-@pytest.mark.parametrize("path", PATHS)
+@pytest.mark.parametrize("path", KNN_PATHS)
 @pytest.mark.parametrize("name,make,k", KNN_CASES, ids=[c[0] for c in KNN_CASES])
 def test_knn_bit_exact_vs_oracle(ctx, path, name, make, k):
     X = make()
+    if path in (_culof.PATH_FAST, _culof.PATH_TENSOR) and (k > 64 or X.shape[1] > 128):
+        pytest.skip("the fused paths take k <= 64 and d <= 128")
     ctx.set_path(path)
     idx, d2, kd = run_knn(ctx, X, k)
     Xc, _, _ = oracle.center(X)
@@ -104,7 +108,7 @@ def test_auto_selects_the_fast_path_for_small_d(ctx):
     ctx.lof(synthetic.reference_test_data(600, 4, seed=5), 257)
     assert ctx.last_path() == _culof.PATH_GENERAL
     ctx.lof(synthetic.reference_test_data(600, 32, seed=5), 20)
-    assert ctx.last_path() == _culof.PATH_FAST
+    assert ctx.last_path() == _culof.PATH_TENSOR
     ctx.lof(synthetic.reference_test_data(600, 200, seed=5), 20)
     assert ctx.last_path() == _culof.PATH_GENERAL
 
