@@ -80,7 +80,7 @@ private:
     DevBuf nbr_idx_, nbr_d2_, kdist2_, lrd_, scores_, nof_, labels_, offset_, offset_scratch_;
     DevBuf tile_;
     // fast path workspaces
-    DevBuf morton_, perm_, sort_tmp_, sort_hist_, cols_, rows_;
+    DevBuf morton_, perm_, sort_tmp_, sort_hist_, cols_, rows_, tc_lists_;
     // Device status word of the current call: kernels set it (a bounded wait
     // that expired, an out-of-range neighbour index); host paths check it.
     DevBuf status_;

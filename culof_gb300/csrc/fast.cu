@@ -723,7 +723,9 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
     const int64_t padded = static_cast<int64_t>(nt) * kCT;
     int sms = 152;
     CG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_));
-    const int nsplit = nt > 1 ? choose_splits(nt, sms) : 1;
+    // The tensor sweep runs two CTAs per SM; with two or more waves of row
+    // tiles a single column split keeps each row's final rescoring to one pass.
+    const int nsplit = nt <= 1 ? 1 : (tensor && nt >= 4 * sms) ? 1 : choose_splits(nt, sms);
 
     // 1. Morton keys of the centred coordinates, then a stable radix sort.
     unsigned* mm = reinterpret_cast<unsigned*>(sort_hist_.get(2 * sizeof(unsigned) * d + sizeof(int) * kMortonDims));
@@ -802,7 +804,8 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
 
     // 4. sweep over the other tiles, split S ways
     if (nt > 1 && tensor) {
-        tc_sweep(tcb, nt, nsplit, d, k, maxn, kth_shared, partial, status, s);
+        uint64_t* lists = static_cast<uint64_t*>(tc_lists_.get(tc_list_bytes(nt, nsplit)));
+        tc_sweep(tcb, nt, nsplit, d, k, maxn, kth_shared, partial, lists, status, s);
     } else if (nt > 1 && wide) {
         wide_sweep(tiles, nt, nsplit, d, k, maxn, kth_shared, partial, s);
     } else if (nt > 1) {

@@ -43,7 +43,9 @@ TcBuffers tc_prepare(void* buf, const float* xc, const float* norms, int64_t n, 
                      const unsigned* minmax, cudaStream_t s);
 void tc_seed(const TcBuffers& b, int nt, int d, int k, uint64_t* seed_keys, unsigned long long* kth_shared,
              cudaStream_t s);
+// Workspace of the per-row lists of one sweep launch batch.
+size_t tc_list_bytes(int nt, int nsplit);
 void tc_sweep(const TcBuffers& b, int nt, int nsplit, int d, int k, const unsigned* maxn,
-              unsigned long long* kth_shared, uint64_t* partial, int* status, cudaStream_t s);
+              unsigned long long* kth_shared, uint64_t* partial, uint64_t* lists, int* status, cudaStream_t s);
 
 }  // namespace culof_gb300

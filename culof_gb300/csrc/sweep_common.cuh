@@ -129,7 +129,7 @@ template <int M>
 __device__ void compact_row(RowLists<M>& L, int r, int k, float nmax, int dp) {
     // the bitonic network needs a power of two: pad M/32 registers up (with kKeyMax)
     constexpr int E = (M / 32) <= 1 ? 1 : (M / 32) <= 2 ? 2 : (M / 32) <= 4 ? 4 : 8;
-    static_assert(M % 32 == 0 && M <= 256, "list capacity");
+    static_assert(M % 8 == 0 && M <= 256, "list capacity");
     const int lane = threadIdx.x & 31;
     const int c = min(L.cnt[r], M);
     uint64_t v[E];

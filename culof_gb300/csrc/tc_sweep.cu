@@ -13,19 +13,28 @@
 //     epilogue warps read the accumulator back (thread = row), evaluate
 //     f = |b|^2 - 2 a.b with packed fma.rn.f32x2 and compare it with the
 //     row's threshold tau (sign of a packed subtract);
-//   * passing pairs are queued per warp and rescored exactly from FP32
-//     row-major coordinates (the oracle's direct-difference formula) into
-//     per-row lists; compaction, the shared k-th key and the merge are those
-//     of the FP32 sweeps.
+//   * a passing pair's (f, column) enters the row's list directly (the
+//     row's own thread appends it; no global memory is read). Lists are
+//     compacted by f: with fk the k-th smallest f in the list, every entry
+//     above a proven margin over fk (approx_thr) is strictly farther than
+//     k listed columns and is dropped, and the filter threshold tightens to
+//     that margin;
+//   * at the end each row's surviving entries (about k) are rescored exactly
+//     from FP32 row-major coordinates (the oracle's direct-difference chain;
+//     coalesced column loads, differences staged in the freed operand
+//     buffers) and reduced to the exact k best keys, which the merge of the
+//     FP32 sweeps combines with the seed list. A row whose list would
+//     overflow with entries inside the margin (heavy duplicates) switches to
+//     exact lists: its candidates are then rescored as they pass.
 //
-// Exactness: tau (tc_tau below) bounds the filter value of every column whose
-// exact FP32 distance can still enter the row's k best, covering the f16
-// rounding of both operands (relative 2^-11, absolute 2^-14 in scaled units
-// for values that fall below the f16 normal range or are flushed), the f32
-// accumulation of the tensor core (taken as K * 2^-20 relative), the float32
-// norms and the float32 evaluation of f. Data whose scale cannot be brought
-// into the f16 range (|S| > 62, or non-finite values) disable the filter:
-// every pair is then rescored exactly.
+// Exactness: the thresholds (row_bounds below) cover the f16 rounding of
+// both operands (relative 2^-11, absolute 2^-14 in scaled units for values
+// that fall below the f16 normal range or are flushed), the f32 accumulation
+// of the tensor core (taken as K * 2^-20 relative), the float32 norms and
+// the float32 evaluation of f, so no column that belongs to a row's k
+// nearest is ever dropped. Data whose scale cannot be brought into the f16
+// range (|S| > 62, or non-finite values) disable the filter: every pair is
+// then rescored exactly.
 #include <cuda_fp16.h>
 
 #include "common.cuh"
@@ -44,6 +53,7 @@ constexpr int kTcStages = 2;
 constexpr int kEpiWarps = 4;
 constexpr int kTcThreads = 32 * (2 + kEpiWarps);  // producer, MMA, 4 epilogue warps
 constexpr int kTcQueue = 32 + 32 * 32;            // a drain chunk + one 32-column chunk of every lane
+constexpr int kTcM = 128;                         // list capacity per row (k <= 64)
 constexpr int kBox = 128 * 128;                   // bytes of one TMA box: 128 rows x 64 f16
 constexpr int kTmemCols = 256;                    // two 128-column f32 accumulators
 
@@ -161,33 +171,61 @@ __global__ void __launch_bounds__(256) tc_seed_kernel(const float* __restrict__ 
     }
 }
 
-// Rigorous threshold of the f16 filter for a row with float32 norm na whose
-// current k-th key is kth (see the file comment). With D the k-th distance,
-// u = 2^-24, g the relative error of the float32 norms, A, B upper bounds of
-// |a| and |b|, the f16 Gram value G of a column b with exact distance <= D
-// satisfies
-//   |b|^2 - 2 a.b <= Tm - |a|^2,  Tm = D / (1 - (K + 2) u)
+// ---- thresholds ---------------------------------------------------------------
+// Per row a (float32 norm na, K = Kp terms, u = 2^-24, g the relative error of
+// the float32 norms, A >= |a|, B >= |b| for every column b), the f16 Gram value
+// G of a column b and its filter value f = fl(Nb - 2 G) satisfy
 //   |G - a.b| <= E = (2 uh + uh^2) A B + eta (1 + uh) sqrt(K) (A + B) + K eta^2
 //                    + K ua ((1 + uh) A + sqrt(K) eta) ((1 + uh) B + sqrt(K) eta)
-// so f = fl(Nb - 2 G) <= Tm - na / (1 + g) + g / (1 - g) Nmax + 2 E
-//                        + u (Nmax + 2 (A B + E)),
-// plus 8u of slack for evaluating this in double and rounding it up.
-__device__ float tc_tau(uint64_t kth, float na, float nmax, int K, float eta_f) {
-    if (kth == kKeyMax) return __int_as_float(0x7f800000);
-    const double D = static_cast<double>(__uint_as_float(key_bits(kth)));
-    const double u = 5.9604644775390625e-08;  // 2^-24
-    const double uh = 4.8828125e-04;          // 2^-11
-    const double ua = 9.5367431640625e-07;    // 2^-20
-    const double g = (K + 1) * u / (1.0 - (K + 1) * u);
-    const double a = static_cast<double>(na), m = static_cast<double>(nmax), eta = static_cast<double>(eta_f);
-    const double Tm = D / (1.0 - (K + 2) * u);
+//   |f - (|b|^2 - 2 a.b)| <= m0 = g / (1 - g) Nmax + 2 E + u (Nmax + 2 (A B + E))
+// (uh = 2^-11 the f16 rounding, eta the absolute f16 error, ua = 2^-20 per
+// accumulated term of the tensor core). Two consequences, each evaluated with
+// upward rounding:
+//  * exact threshold: a column whose exact float32 distance is <= D has
+//    f <= D c1 + c0 (c1 = (1 + 8u) / (1 - (K + 2) u),
+//    c0 = -na / (1 + g) + m0 + 8u (na + Nmax + 2 A B));
+//  * approximate threshold: with T the real squared distance and
+//    D in T [1 - dl, 1 + dl] (dl = (K + 3) u / (1 - (K + 3) u)), a column b with
+//    f_b > thr(fk) = fk + 2 m0 + 2 dl / (1 - dl) max(0, fk + na / (1 - g) + m0)
+//    (+ slack) is strictly farther than every column c with f_c <= fk, so once
+//    k columns with f <= fk are known, b can never be among the k nearest.
+struct RowBounds {
+    float c0, c3, c4;  // per row: exact offset; approximate offset and shift
+};
+constexpr double kU = 5.9604644775390625e-08;  // 2^-24
+
+__device__ RowBounds row_bounds(float na_f, float nmax_f, int K, float eta_f) {
+    const double uh = 4.8828125e-04;        // 2^-11
+    const double ua = 9.5367431640625e-07;  // 2^-20
+    const double g = (K + 1) * kU / (1.0 - (K + 1) * kU);
+    const double a = static_cast<double>(na_f), m = static_cast<double>(nmax_f), eta = static_cast<double>(eta_f);
     const double A = sqrt(a / (1.0 - g)), B = sqrt(m / (1.0 - g));
     const double sk = sqrt(static_cast<double>(K));
     const double E = (2.0 * uh + uh * uh) * A * B + eta * (1.0 + uh) * sk * (A + B) + K * eta * eta +
                      K * ua * ((1.0 + uh) * A + sk * eta) * ((1.0 + uh) * B + sk * eta);
-    double t = Tm - a / (1.0 + g) + g / (1.0 - g) * m + 2.0 * E + u * (m + 2.0 * (A * B + E));
-    t += 8.0 * u * (Tm + a + m + 2.0 * A * B) + 1e-30;
-    return __double2float_ru(t);
+    const double m0 = g / (1.0 - g) * m + 2.0 * E + kU * (m + 2.0 * (A * B + E));
+    const double slack = 8.0 * kU * (a + m + 2.0 * A * B) + 1e-30;
+    RowBounds r;
+    r.c0 = __double2float_ru(-a / (1.0 + g) + m0 + slack);
+    r.c3 = __double2float_ru(2.0 * m0 + slack);
+    r.c4 = __double2float_ru(a / (1.0 - g) + m0);
+    return r;
+}
+__device__ __forceinline__ float exact_c1(int K) {
+    return __double2float_ru((1.0 + 8.0 * kU) / (1.0 - (K + 2) * kU));
+}
+__device__ __forceinline__ float approx_c2(int K) {
+    const double dl = (K + 3) * kU / (1.0 - (K + 3) * kU);
+    return __double2float_ru(2.0 * dl / (1.0 - dl) * (1.0 + 8.0 * kU));
+}
+// Filter threshold of a row from its exact k-th key.
+__device__ __forceinline__ float exact_tau(uint64_t kth, float c1, float c0) {
+    if (kth == kKeyMax) return __int_as_float(0x7f800000);
+    return __fmaf_ru(__uint_as_float(key_bits(kth)), c1, c0);
+}
+// The approximate threshold over a k-th filter value fk.
+__device__ __forceinline__ float approx_thr(float fk, float c2, float c3, float c4) {
+    return __fadd_ru(fk, __fmaf_ru(fmaxf(0.0f, __fadd_ru(fk, c4)), c2, c3));
 }
 
 __device__ __forceinline__ uint64_t tau_pair(float tau) {
@@ -208,48 +246,191 @@ __device__ __forceinline__ uint64_t pack2(float lo, float hi) {
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
+// Order-preserving bits of a float (negative values included).
+__device__ __forceinline__ uint32_t flip_bits(float f) {
+    const uint32_t u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
 
-template <int M>
+// Row modes: approximate lists hold (flip(f) << 32 | sorted column position);
+// exact lists hold the usual (distance bits << 32 | original index).
+constexpr int kModeApprox = 0;
+constexpr int kModeExact = 1;
+
+// Per-row lists live in global memory (L2-resident while their CTA runs):
+// kTcM keys per row, 128 rows per CTA. Keeping them out of shared memory
+// lets two CTAs share an SM, so two epilogue warps per SM sub-partition
+// hide each other's latencies.
+constexpr int kTcListRow = kTcM;
+constexpr size_t kTcListCta = static_cast<size_t>(kRT) * kTcListRow;  // keys per CTA
+constexpr int kTcMaxCtasPerLaunch = 4096;                             // bounds the list workspace (512 MiB)
+
 struct TcSmem {
-    uint8_t a[2][kBox];              // row tile operand (K boxes 0..1)
-    uint8_t b[kTcStages][2][kBox];   // column tile operands
-    RowLists<M> L;
-    uint16_t queue[kEpiWarps][kTcQueue];
+    uint8_t a[2][kBox];             // row tile operand (K boxes 0..1)
+    uint8_t b[kTcStages][2][kBox];  // column tile operands
+    uint64_t kth[kRT];              // exact k-th key known for the row (only decreases)
+    float athr[kRT];                // approximate threshold of the row's list (+inf until k entries)
+    float row_norm[kRT];
+    int cnt[kRT];
+    int mode[kRT];
+    uint16_t queue[kEpiWarps][kTcQueue];  // exact-mode candidates (row << 8 | column) of the current tile
+    float nb[kEpiWarps][2][kCT];          // column norms of the current and the next tile, per epilogue warp
     uint64_t full[kTcStages], empty[kTcStages], tfull[2], tempty[2], afull, fin;
     uint32_t tmem_base;
     int abort;
 };
+static_assert(2 * (sizeof(TcSmem) + 1024 + 1024) <= 233472, "two tensor-sweep CTAs must fit on an SM");
+// The final exact rescoring reuses the operand buffers (free once the last MMA
+// has completed): per epilogue warp, 32 candidates x (128 + 1) differences.
+constexpr int kScratchLd = 129;
+static_assert(kEpiWarps * 32 * kScratchLd * 4 <= 3 * 2 * kBox, "scratch fits in the operand buffers");
 
-template <int M>
-__device__ void tc_abort(TcSmem<M>& sh, int* status) {
+__device__ void tc_abort(TcSmem& sh, int* status) {
     *reinterpret_cast<volatile int*>(&sh.abort) = 1;
     atomicExch(status, 1);
 }
-template <int M>
-__device__ __forceinline__ bool tc_aborted(TcSmem<M>& sh) {
-    return *reinterpret_cast<volatile int*>(&sh.abort) != 0;
+__device__ __forceinline__ bool tc_aborted(TcSmem& sh) { return *reinterpret_cast<volatile int*>(&sh.abort) != 0; }
+
+// g[b] for a lane-dependent b, without local memory: a 5-level select tree.
+__device__ __forceinline__ uint32_t select32(const uint32_t (&g)[32], int b) {
+    uint32_t v16[16], v8[8], v4[4], v2[2];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v16[i] = (b & 16) ? g[16 + i] : g[i];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) v8[i] = (b & 8) ? v16[8 + i] : v16[i];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) v4[i] = (b & 4) ? v8[4 + i] : v8[i];
+#pragma unroll
+    for (int i = 0; i < 2; ++i) v2[i] = (b & 2) ? v4[2 + i] : v4[i];
+    return (b & 1) ? v2[1] : v2[0];
 }
 
-// Compact every row of this epilogue warp (32 rows from row0) whose list has
-// less than 32 free slots. True if any was.
-template <int M>
-__device__ bool tc_compact_full_rows(RowLists<M>& L, int row0, int k, float nmax, int dp) {
-    const int lane = threadIdx.x & 31;
-    unsigned full = __ballot_sync(0xffffffffu, L.cnt[row0 + lane] > M - 32);
-    const bool any = full != 0;
-    while (full) {
-        compact_row<M>(L, row0 + __ffs(full) - 1, k, nmax, dp);
-        full &= full - 1;
+// Exact key of (row position pa, column position pb), one lane: the oracle's
+// direct-difference chain over row-major FP32 coordinates.
+__device__ __forceinline__ uint64_t exact_key_lane(const float* __restrict__ xr, const unsigned* __restrict__ ix,
+                                                   int64_t pa, int64_t pb, int d, int dr) {
+    const unsigned ib = __ldg(ix + pb);
+    if (ib == kNoIndex) return kKeyMax;
+    const float4* va = reinterpret_cast<const float4*>(xr + pa * dr);
+    const float4* vb = reinterpret_cast<const float4*>(xr + pb * dr);
+    float s = 0.0f;
+    for (int f4 = 0; 4 * f4 < d; ++f4) {
+        const float4 x = __ldg(va + f4), y = __ldg(vb + f4);
+        const float xa[4] = {x.x, x.y, x.z, x.w}, yb[4] = {y.x, y.y, y.z, y.w};
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            if (4 * f4 + q < d) {
+                const float t = __fsub_rn(xa[q], yb[q]);
+                s = __fmaf_rn(t, t, s);
+            }
+        }
     }
-    return any;
+    return make_key(__float_as_uint(s), ib);
 }
 
-// Rescore the warp's queued pairs of column tile `tile` exactly and add the
-// keys that beat their row's k-th key. True if a list was compacted.
-template <int M>
-__device__ bool tc_drain(TcSmem<M>& sh, int wq, int row0, int qc, int64_t rbase, int64_t cbase,
-                         const float* __restrict__ xr, const unsigned* __restrict__ ix, int d, int dr, int k,
-                         float nmax, int Kp) {
+constexpr int kListE = kTcListRow / 32;  // list keys per lane in a compaction
+static_assert(kListE == 4, "the compaction sorts 4 keys per lane");
+
+// Exact list of row r (whole warp): sort, drop duplicates, keep the k
+// smallest; tighten the row's exact k-th key.
+__noinline__ __device__ void compact_exact(TcSmem& sh, uint64_t* __restrict__ lst, int r, int k) {
+    const int lane = threadIdx.x & 31;
+    const int c = min(sh.cnt[r], kTcListRow);
+    uint64_t v[kListE];
+#pragma unroll
+    for (int j = 0; j < kListE; ++j) {
+        const int e = j * 32 + lane;
+        v[j] = e < c ? lst[e] : kKeyMax;
+    }
+    warp_bitonic_sort<kListE>(v);
+    int rank[kListE];
+    const int uniq = warp_unique_ranks<kListE>(v, kKeyMax, rank);
+    __syncwarp();
+    uint64_t kth_new = kKeyMax;
+#pragma unroll
+    for (int j = 0; j < kListE; ++j) {
+        if (rank[j] >= 0 && rank[j] < k) lst[rank[j]] = v[j];
+        if (rank[j] == k - 1) kth_new = v[j];
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, kth_new != kKeyMax);
+    const uint64_t kk = __shfl_sync(0xffffffffu, kth_new, m ? __ffs(m) - 1 : 0);
+    if (lane == 0) {
+        sh.cnt[r] = min(uniq, k);
+        if (m && kk < sh.kth[r]) sh.kth[r] = kk;
+    }
+    __syncwarp();
+}
+
+// Sort row r's approximate list (whole warp), find its k-th filter value fk
+// and keep the entries with f <= approx_thr(fk) (all of them while fewer than
+// k are known). Returns the number kept; if that exceeds `cap`, the list is
+// left untrimmed and the caller decides.
+__noinline__ __device__ int approx_compact(TcSmem& sh, uint64_t* __restrict__ lst, int r, int k, float c2, float c3,
+                                           float c4, int cap) {
+    const int lane = threadIdx.x & 31;
+    const int c = min(sh.cnt[r], kTcListRow);
+    uint64_t v[kListE];
+#pragma unroll
+    for (int j = 0; j < kListE; ++j) {
+        const int e = j * 32 + lane;
+        v[j] = e < c ? lst[e] : kKeyMax;
+    }
+    warp_bitonic_sort<kListE>(v);
+    float thr = __int_as_float(0x7f800000);
+    if (c >= k) {
+        const int owner = (k - 1) & 31, oreg = (k - 1) >> 5;
+        uint64_t kk = kKeyMax;
+#pragma unroll
+        for (int j = 0; j < kListE; ++j) {
+            const uint64_t t = __shfl_sync(0xffffffffu, v[j], owner);
+            if (j == oreg) kk = t;
+        }
+        thr = approx_thr(unflip(key_bits(kk)), c2, c3, c4);
+    }
+    int keep = 0;
+#pragma unroll
+    for (int j = 0; j < kListE; ++j) {
+        const bool in = v[j] != kKeyMax && unflip(key_bits(v[j])) <= thr;
+        keep += __popc(__ballot_sync(0xffffffffu, in));
+    }
+    if (keep <= cap) {
+#pragma unroll
+        for (int j = 0; j < kListE; ++j) {
+            const int e = j * 32 + lane;
+            if (e < keep) lst[e] = v[j];
+        }
+        if (lane == 0) {
+            sh.cnt[r] = keep;
+            sh.athr[r] = thr;
+        }
+    }
+    __syncwarp();
+    return keep;
+}
+
+// Row r leaves approximate mode (its list would overflow with entries within
+// the approximate margin, e.g. many duplicates): every entry is rescored
+// exactly (one lane per entry) and the list becomes an exact k-best list.
+__noinline__ __device__ void to_exact_mode(TcSmem& sh, uint64_t* __restrict__ lst, int r, int64_t rbase,
+                                           const float* __restrict__ xr, const unsigned* __restrict__ ix, int d,
+                                           int dr, int k) {
+    const int lane = threadIdx.x & 31;
+    const int c = min(sh.cnt[r], kTcListRow);
+    for (int e = lane; e < c; e += 32) {
+        const int64_t pb = static_cast<int64_t>(key_index(lst[e]));
+        lst[e] = exact_key_lane(xr, ix, rbase + r, pb, d, dr);
+    }
+    __syncwarp();
+    if (lane == 0) sh.mode[r] = kModeExact;
+    __syncwarp();
+    compact_exact(sh, lst, r, k);
+}
+
+// Rescore the warp's queued exact-mode pairs of column tile cbase exactly and
+// add the keys that beat their row's k-th key. True if a list was compacted.
+__noinline__ __device__ bool tc_drain(TcSmem& sh, uint64_t* __restrict__ glist, int wq, int row0, int qc,
+                                      int64_t rbase, int64_t cbase, const float* __restrict__ xr,
+                                      const unsigned* __restrict__ ix, int d, int dr, int k) {
     const int lane = threadIdx.x & 31;
     bool compacted = false;
     for (int base = 0; base < qc; base += 32) {
@@ -257,46 +438,88 @@ __device__ bool tc_drain(TcSmem<M>& sh, int wq, int row0, int qc, int64_t rbase,
         if (i < qc) {
             const unsigned e = sh.queue[wq][i];
             const int r = static_cast<int>(e >> 8), c = static_cast<int>(e & 0xFF);
-            const unsigned ib = __ldg(ix + cbase + c);
-            if (ib != kNoIndex) {
-                const float4* pa = reinterpret_cast<const float4*>(xr + (rbase + r) * dr);
-                const float4* pb = reinterpret_cast<const float4*>(xr + (cbase + c) * dr);
-                float s = 0.0f;
-                for (int f4 = 0; 4 * f4 < d; ++f4) {
-                    const float4 x = __ldg(pa + f4), y = __ldg(pb + f4);
-                    const float xa[4] = {x.x, x.y, x.z, x.w}, yb[4] = {y.x, y.y, y.z, y.w};
-#pragma unroll
-                    for (int q = 0; q < 4; ++q) {
-                        if (4 * f4 + q < d) {
-                            const float t = __fsub_rn(xa[q], yb[q]);
-                            s = __fmaf_rn(t, t, s);
-                        }
-                    }
-                }
-                const uint64_t key = make_key(__float_as_uint(s), ib);
-                if (key < sh.L.kth[r]) {
-                    const int slot = atomicAdd(&sh.L.cnt[r], 1);
-                    sh.L.list[r][slot] = key;
-                }
+            const uint64_t key = exact_key_lane(xr, ix, rbase + r, cbase + c, d, dr);
+            if (key < sh.kth[r]) {
+                const int slot = atomicAdd(&sh.cnt[r], 1);
+                glist[static_cast<size_t>(r) * kTcListRow + slot] = key;
             }
         }
         __syncwarp();
-        compacted |= tc_compact_full_rows<M>(sh.L, row0, k, nmax, Kp);
+        unsigned full = __ballot_sync(0xffffffffu,
+                                      sh.mode[row0 + lane] == kModeExact && sh.cnt[row0 + lane] > kTcListRow - 32);
+        compacted |= full != 0;
+        while (full) {
+            const int rr = row0 + __ffs(full) - 1;
+            full &= full - 1;
+            compact_exact(sh, glist + static_cast<size_t>(rr) * kTcListRow, rr, k);
+        }
     }
     return compacted;
 }
 
-template <int M>
-__global__ void __launch_bounds__(kTcThreads, 1)
+// Final exact rescoring of the first P approximate entries of row r (whole
+// warp): lane l loads dimensions 4l..4l+3 of each candidate column with one
+// coalesced 512-byte warp load per column, forms the differences t = a - b
+// and stages them in shared memory; lane i then runs candidate i's FMA chain
+// in dimension order (bit-identical to the oracle's formula).
+__noinline__ __device__ void rescore_final(uint64_t* __restrict__ lst, int r, int P, float* __restrict__ scratch,
+                                           int64_t rbase, const float* __restrict__ xr,
+                                           const unsigned* __restrict__ ix, int d, int dr) {
+    const int lane = threadIdx.x & 31;
+    const bool has = 4 * lane < dr;
+    const float4 a4 = has ? __ldg(reinterpret_cast<const float4*>(xr + (rbase + r) * dr) + lane)
+                          : make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int base = 0; base < P; base += 32) {
+        const int nb = min(32, P - base);
+        const uint32_t mypos = lane < nb ? key_index(lst[base + lane]) : 0u;
+        for (int i0 = 0; i0 < nb; i0 += 8) {
+            float4 b4[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                const int i = i0 + q;
+                const uint32_t pb = __shfl_sync(0xffffffffu, mypos, i & 31);
+                b4[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (i < nb && has) b4[q] = __ldg(reinterpret_cast<const float4*>(xr + static_cast<int64_t>(pb) * dr) + lane);
+            }
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                float* t = scratch + (i0 + q) * kScratchLd + 4 * lane;
+                if (i0 + q < nb && has) {
+                    t[0] = __fsub_rn(a4.x, b4[q].x);
+                    t[1] = __fsub_rn(a4.y, b4[q].y);
+                    t[2] = __fsub_rn(a4.z, b4[q].z);
+                    t[3] = __fsub_rn(a4.w, b4[q].w);
+                }
+            }
+        }
+        __syncwarp();
+        uint64_t key = kKeyMax;
+        if (lane < nb) {
+            const unsigned ib = __ldg(ix + mypos);
+            if (ib != kNoIndex) {
+                const float* t = scratch + lane * kScratchLd;
+                float s = 0.0f;
+                for (int f = 0; f < d; ++f) s = __fmaf_rn(t[f], t[f], s);
+                key = make_key(__float_as_uint(s), ib);
+            }
+        }
+        __syncwarp();
+        if (lane < nb) lst[base + lane] = key;
+        __syncwarp();
+    }
+}
+
+__global__ void __launch_bounds__(kTcThreads, 2)
 tc_sweep_kernel(const __grid_constant__ CUtensorMap tmap, const float* __restrict__ xr,
                 const float* __restrict__ cn, const unsigned* __restrict__ ix, const TcScale* __restrict__ scale,
-                int nt, int nsplit, int d, int dr, int Kp, int k, const unsigned* __restrict__ max_norm_bits,
-                unsigned long long* __restrict__ kth_shared, uint64_t* __restrict__ partial, int* __restrict__ status) {
+                int nt, int T0, int ntb, int nsplit, int d, int dr, int Kp, int k,
+                const unsigned* __restrict__ max_norm_bits, unsigned long long* __restrict__ kth_shared,
+                uint64_t* __restrict__ partial, uint64_t* __restrict__ lists, int* __restrict__ status) {
     extern __shared__ uint8_t tc_raw[];
-    TcSmem<M>& sh = *reinterpret_cast<TcSmem<M>*>((reinterpret_cast<uintptr_t>(tc_raw) + 1023) & ~uintptr_t(1023));
+    TcSmem& sh = *reinterpret_cast<TcSmem*>((reinterpret_cast<uintptr_t>(tc_raw) + 1023) & ~uintptr_t(1023));
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int T = blockIdx.x % nt;
-    const int split = blockIdx.x / nt;
+    const int T = T0 + static_cast<int>(blockIdx.x) % ntb;
+    const int split = static_cast<int>(blockIdx.x) / ntb;
     const int per = (nt - 1 + nsplit - 1) / nsplit;
     const int q0 = 1 + split * per;
     const int q1 = min(nt, q0 + per);
@@ -304,6 +527,7 @@ tc_sweep_kernel(const __grid_constant__ CUtensorMap tmap, const float* __restric
     const int nkb = Kp / 64;
     const float nmax = __uint_as_float(*max_norm_bits);
     const int64_t rbase = static_cast<int64_t>(T) * kRT;
+    uint64_t* glist = lists + static_cast<size_t>(blockIdx.x) * kTcListCta;
 
     if (tid == 0) {
         for (int s = 0; s < kTcStages; ++s) {
@@ -322,10 +546,12 @@ tc_sweep_kernel(const __grid_constant__ CUtensorMap tmap, const float* __restric
     if (warp == 1) tc::tmem_alloc(&sh.tmem_base, kTmemCols);
     if (warp >= 2) {
         const int r = 32 * (warp & 3) + lane;
-        sh.L.kth[r] = kth_shared[rbase + r];
-        sh.L.row_norm[r] = cn[rbase + r];
-        sh.L.tau[r] = 0.0f;
-        sh.L.cnt[r] = 0;
+        sh.kth[r] = kth_shared[rbase + r];
+        sh.row_norm[r] = cn[rbase + r];
+        sh.cnt[r] = 0;
+        sh.athr[r] = __int_as_float(0x7f800000);
+        // with the filter disabled the f values carry no information: exact lists
+        sh.mode[r] = scale->all != 0.0f ? kModeExact : kModeApprox;
     }
     tc::tc_fence_before();
     __syncthreads();
@@ -390,87 +616,164 @@ tc_sweep_kernel(const __grid_constant__ CUtensorMap tmap, const float* __restric
         const int wq = warp - 2;
         const int row0 = 32 * (warp & 3);
         const int r = row0 + lane;
+        uint64_t* const mylist = glist + static_cast<size_t>(r) * kTcListRow;
         const TcScale sc = *scale;
         const bool all = sc.all != 0.0f;
         const bool row_valid = __ldg(ix + rbase + r) != kNoIndex;
-        const float na = sh.L.row_norm[r];
+        const RowBounds rb = row_bounds(sh.row_norm[r], nmax, Kp, sc.eta);
+        const float c1 = exact_c1(Kp), c2 = approx_c2(Kp);
         auto row_tau = [&]() -> float {
-            return row_valid ? tc_tau(sh.L.kth[r], na, nmax, Kp, sc.eta) : __int_as_float(0xff800000);
+            if (!row_valid) return __int_as_float(0xff800000);
+            float t = exact_tau(sh.kth[r], c1, rb.c0);
+            if (sh.mode[r] == kModeApprox) t = fminf(t, sh.athr[r]);
+            return t;
         };
         uint64_t tq = tau_pair(row_tau());
         const uint64_t k2 = dup2(sc.k2);
         const uint32_t lane_addr = tmem + (static_cast<uint32_t>(row0) << 16);
+        // This tile's column norms are staged in a per-warp shared ring one
+        // tile ahead (one coalesced 512-byte load per warp), so the filter
+        // never waits on global memory.
+        auto tile_base = [&](int jj) -> int64_t { return static_cast<int64_t>(spiral_tile(T, q0 + jj, nt)) * kCT; };
+        float4 npre = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (count > 0) npre = __ldg(reinterpret_cast<const float4*>(cn + tile_base(0)) + lane);
+        int qc = 0;
+        int64_t cbase = 0;
+        const float* nbj = nullptr;
+        // filter one 32-column chunk held in registers; list / queue its candidates
+        auto process_chunk = [&](const uint32_t (&gr)[32], int ch) {
+            uint64_t dl[16];
+            unsigned signs = 0;
+            const float4* nb4 = reinterpret_cast<const float4*>(nbj + 32 * ch);
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                const float4 nb = nb4[q];
+                const uint64_t f0 = fma2(pack2(__uint_as_float(gr[4 * q]), __uint_as_float(gr[4 * q + 1])), k2,
+                                         pack2(nb.x, nb.y));
+                const uint64_t f1 = fma2(pack2(__uint_as_float(gr[4 * q + 2]), __uint_as_float(gr[4 * q + 3])), k2,
+                                         pack2(nb.z, nb.w));
+                dl[2 * q] = sub2(f0, tq);
+                dl[2 * q + 1] = sub2(f1, tq);
+                signs |= static_cast<unsigned>(dl[2 * q]) | static_cast<unsigned>(dl[2 * q] >> 32) |
+                         static_cast<unsigned>(dl[2 * q + 1]) | static_cast<unsigned>(dl[2 * q + 1] >> 32);
+            }
+            if (all) signs = row_valid ? 0x80000000u : 0u;
+            if (!__any_sync(0xffffffffu, static_cast<int>(signs) < 0)) return;
+            unsigned pass = 0;
+            if (all) {
+                pass = row_valid ? 0xFFFFFFFFu : 0u;
+            } else {
+#pragma unroll
+                for (int q = 0; q < 16; ++q) {
+                    pass |= (static_cast<unsigned>(dl[q]) >> 31) << (2 * q);
+                    pass |= static_cast<unsigned>(dl[q] >> 63) << (2 * q + 1);
+                }
+            }
+            const bool exact_row = sh.mode[r] == kModeExact;
+            if (!exact_row && pass) {
+                // approximate keys straight into the row's own list (f
+                // recomputed exactly as the packed filter did)
+                int cnt = sh.cnt[r];
+                unsigned pp = pass;
+                while (pp) {
+                    const int b = __ffs(pp) - 1;
+                    pp &= pp - 1;
+                    const float f = __fmaf_rn(__uint_as_float(select32(gr, b)), sc.k2, nbj[32 * ch + b]);
+                    mylist[cnt++] = make_key(flip_bits(f), static_cast<uint32_t>(cbase + 32 * ch + b));
+                }
+                sh.cnt[r] = cnt;
+            }
+            if (__any_sync(0xffffffffu, exact_row && pass)) {
+                int tot;
+                int off = warp_prefix_offset(exact_row ? __popc(pass) : 0, tot);
+                if (exact_row) {
+                    unsigned pp = pass;
+                    while (pp) {
+                        const int b = __ffs(pp) - 1;
+                        pp &= pp - 1;
+                        sh.queue[wq][qc + off++] = static_cast<uint16_t>((r << 8) | (32 * ch + b));
+                    }
+                }
+                qc += tot;
+            }
+            __syncwarp();
+            // keep room for the next chunk: compact approximate lists with
+            // less than 32 free slots
+            unsigned full =
+                __ballot_sync(0xffffffffu, sh.mode[r] == kModeApprox && sh.cnt[r] > kTcListRow - 32);
+            bool changed = full != 0;
+            while (full) {
+                const int src = __ffs(full) - 1;
+                full &= full - 1;
+                const int rr = row0 + src;
+                uint64_t* lst = glist + static_cast<size_t>(rr) * kTcListRow;
+                const float c3 = __shfl_sync(0xffffffffu, rb.c3, src);
+                const float c4 = __shfl_sync(0xffffffffu, rb.c4, src);
+                if (approx_compact(sh, lst, rr, k, c2, c3, c4, kTcListRow - 32) > kTcListRow - 32)
+                    to_exact_mode(sh, lst, rr, rbase, xr, ix, d, dr, k);
+            }
+            if (qc >= 32) {
+                changed |= tc_drain(sh, glist, wq, row0, qc, rbase, cbase, xr, ix, d, dr, k);
+                qc = 0;
+            }
+            if (changed) tq = tau_pair(row_tau());
+        };
         for (int j = 0; j < count; ++j) {
             const int acc = j & 1;
+            cbase = tile_base(j);
+            float* nbw = sh.nb[wq][j & 1];
+            reinterpret_cast<float4*>(nbw)[lane] = npre;
+            if (j + 1 < count) npre = __ldg(reinterpret_cast<const float4*>(cn + tile_base(j + 1)) + lane);
+            nbj = nbw;
+            __syncwarp();
             if (!mbar_wait_warp(&sh.tfull[acc], (j >> 1) & 1)) {
                 if (lane == 0) tc_abort(sh, status);
                 break;
             }
             tc::tc_fence_after();
-            const int64_t cbase = static_cast<int64_t>(spiral_tile(T, q0 + j, nt)) * kCT;
-            const float4* cn4 = reinterpret_cast<const float4*>(cn + cbase);
-            int qc = 0;
+            qc = 0;
+            // chunk ch + 1 streams out of TMEM while chunk ch is filtered
+            const uint32_t taddr = lane_addr + static_cast<uint32_t>(acc * 128);
+            uint32_t ga[32], gb[32];
+            tc::tmem_ld32_async(taddr, ga);
 #pragma unroll 1
-            for (int ch = 0; ch < 4; ++ch) {
-                float g[32];
-                tc::tmem_ld32(lane_addr + static_cast<uint32_t>(acc * 128 + 32 * ch), g);
-                uint64_t dl[16];
-                unsigned signs = 0;
-#pragma unroll
-                for (int q = 0; q < 8; ++q) {
-                    const float4 nb = __ldg(cn4 + 8 * ch + q);
-                    const uint64_t f0 = fma2(pack2(g[4 * q], g[4 * q + 1]), k2, pack2(nb.x, nb.y));
-                    const uint64_t f1 = fma2(pack2(g[4 * q + 2], g[4 * q + 3]), k2, pack2(nb.z, nb.w));
-                    dl[2 * q] = sub2(f0, tq);
-                    dl[2 * q + 1] = sub2(f1, tq);
-                    signs |= static_cast<unsigned>(dl[2 * q]) | static_cast<unsigned>(dl[2 * q] >> 32) |
-                             static_cast<unsigned>(dl[2 * q + 1]) | static_cast<unsigned>(dl[2 * q + 1] >> 32);
-                }
-                if (all) signs = row_valid ? 0x80000000u : 0u;
-                if (__any_sync(0xffffffffu, static_cast<int>(signs) < 0)) {
-                    unsigned pass = 0;
-                    if (all) {
-                        pass = row_valid ? 0xFFFFFFFFu : 0u;
-                    } else {
-#pragma unroll
-                        for (int q = 0; q < 16; ++q) {
-                            pass |= (static_cast<unsigned>(dl[q]) >> 31) << (2 * q);
-                            pass |= static_cast<unsigned>(dl[q] >> 63) << (2 * q + 1);
-                        }
-                    }
-                    int tot;
-                    int off = warp_prefix_offset(__popc(pass), tot);
-                    while (pass) {
-                        const int b = __ffs(pass) - 1;
-                        pass &= pass - 1;
-                        sh.queue[wq][qc + off++] = static_cast<uint16_t>((r << 8) | (32 * ch + b));
-                    }
-                    qc += tot;
-                    __syncwarp();
-                    if (qc >= 32) {
-                        if (tc_drain<M>(sh, wq, row0, qc, rbase, cbase, xr, ix, d, dr, k, nmax, Kp))
-                            tq = tau_pair(row_tau());
-                        qc = 0;
-                    }
-                }
+            for (int ch = 0; ch < 4; ch += 2) {
+                tc::tmem_wait32(ga);
+                tc::tmem_ld32_async(taddr + static_cast<uint32_t>(32 * (ch + 1)), gb);
+                process_chunk(ga, ch);
+                tc::tmem_wait32(gb);
+                if (ch + 2 < 4) tc::tmem_ld32_async(taddr + static_cast<uint32_t>(32 * (ch + 2)), ga);
+                process_chunk(gb, ch + 1);
             }
             // the accumulator is free for the next tile but one
             tc::tc_fence_before();
             __syncwarp();
             if (lane == 0) mbar_arrive(&sh.tempty[acc]);
-            if (qc > 0 && tc_drain<M>(sh, wq, row0, qc, rbase, cbase, xr, ix, d, dr, k, nmax, Kp))
-                tq = tau_pair(row_tau());
+            if (qc > 0 && tc_drain(sh, glist, wq, row0, qc, rbase, cbase, xr, ix, d, dr, k)) tq = tau_pair(row_tau());
         }
-        // this split's sorted k best per row; share the k-th key
+        // ---- final: exact k best of this split per row; share the k-th key.
+        // The operand buffers are free once every epilogue warp has read its
+        // last accumulator (the MMAs that read them have completed).
+        asm volatile("bar.sync 1, %0;" ::"r"(32 * kEpiWarps) : "memory");
+        float* scratch = reinterpret_cast<float*>(&sh.a[0][0]) + wq * 32 * kScratchLd;
         for (int i = 0; i < 32; ++i) {
             const int rr = row0 + i;
-            compact_row<M>(sh.L, rr, k, nmax, Kp);
+            uint64_t* lst = glist + static_cast<size_t>(rr) * kTcListRow;
+            if (sh.mode[rr] == kModeApprox) {
+                const float c3 = __shfl_sync(0xffffffffu, rb.c3, i);
+                const float c4 = __shfl_sync(0xffffffffu, rb.c4, i);
+                const int P = approx_compact(sh, lst, rr, k, c2, c3, c4, kTcListRow);
+                rescore_final(lst, rr, P, scratch, rbase, xr, ix, d, dr);
+                if (lane == 0) sh.mode[rr] = kModeExact;
+                __syncwarp();
+            }
+            compact_exact(sh, lst, rr, k);
             const int64_t pos = rbase + rr;
-            const int c = sh.L.cnt[rr];
+            const int c = sh.cnt[rr];
             uint64_t* out = partial + (static_cast<int64_t>(split) * nt * kRT + pos) * k;
-            for (int e = lane; e < k; e += 32) out[e] = e < c ? sh.L.list[rr][e] : kKeyMax;
-            if (lane == 0 && sh.L.kth[rr] != kKeyMax)
-                atomicMin(&kth_shared[pos], static_cast<unsigned long long>(sh.L.kth[rr]));
+            for (int e = lane; e < k; e += 32) out[e] = e < c ? lst[e] : kKeyMax;
+            if (lane == 0 && sh.kth[rr] != kKeyMax)
+                atomicMin(&kth_shared[pos], static_cast<unsigned long long>(sh.kth[rr]));
         }
     }
     tc::tc_fence_before();
@@ -481,23 +784,6 @@ tc_sweep_kernel(const __grid_constant__ CUtensorMap tmap, const float* __restric
     }
 }
 
-template <int M>
-void launch_tc_sweep_m(const TcBuffers& b, int nt, int nsplit, int d, int k, const unsigned* maxn,
-                       unsigned long long* kth_shared, uint64_t* partial, int* status, cudaStream_t s) {
-    const size_t smem = sizeof(TcSmem<M>) + 1024;
-    static bool configured = false;
-    if (!configured) {
-        CG_CUDA(cudaFuncSetAttribute(tc_sweep_kernel<M>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     static_cast<int>(smem)));
-        configured = true;
-    }
-    const CUtensorMap map = tc::make_kmajor_map(b.xh, static_cast<int64_t>(nt) * kCT, b.Kp, true);
-    tc_sweep_kernel<M><<<nt * nsplit, kTcThreads, smem, s>>>(map, b.xr, b.cn, b.ix,
-                                                            reinterpret_cast<const TcScale*>(b.scale), nt, nsplit, d,
-                                                            b.dr, b.Kp, k, maxn, kth_shared, partial, status);
-    CG_LAUNCH_CHECK();
-}
-
 }  // namespace
 
 size_t tc_buffer_bytes(int64_t padded, int d) {
@@ -506,6 +792,12 @@ size_t tc_buffer_bytes(int64_t padded, int d) {
     const auto up = [](size_t x) { return (x + 255) & ~static_cast<size_t>(255); };
     return up(sizeof(__half) * padded * Kp) + up(sizeof(float) * padded * dr) + up(sizeof(float) * padded) +
            up(sizeof(unsigned) * padded) + up(sizeof(TcScale));
+}
+
+size_t tc_list_bytes(int nt, int nsplit) {
+    int64_t ctas = static_cast<int64_t>(nt) * nsplit;
+    if (ctas > kTcMaxCtasPerLaunch) ctas = kTcMaxCtasPerLaunch;
+    return sizeof(uint64_t) * kTcListCta * static_cast<size_t>(ctas);
 }
 
 TcBuffers tc_prepare(void* buf, const float* xc, const float* norms, int64_t n, int d, const unsigned* perm, int nt,
@@ -549,9 +841,25 @@ void tc_seed(const TcBuffers& b, int nt, int d, int k, uint64_t* seed_keys, unsi
 }
 
 void tc_sweep(const TcBuffers& b, int nt, int nsplit, int d, int k, const unsigned* maxn,
-              unsigned long long* kth_shared, uint64_t* partial, int* status, cudaStream_t s) {
-    if (k > 32) launch_tc_sweep_m<96>(b, nt, nsplit, d, k, maxn, kth_shared, partial, status, s);
-    else launch_tc_sweep_m<64>(b, nt, nsplit, d, k, maxn, kth_shared, partial, status, s);
+              unsigned long long* kth_shared, uint64_t* partial, uint64_t* lists, int* status, cudaStream_t s) {
+    const size_t smem = sizeof(TcSmem) + 1024;
+    static bool configured = false;
+    if (!configured) {
+        CG_CUDA(cudaFuncSetAttribute(tc_sweep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     static_cast<int>(smem)));
+        configured = true;
+    }
+    const CUtensorMap map = tc::make_kmajor_map(b.xh, static_cast<int64_t>(nt) * kCT, b.Kp, true);
+    // row tiles in batches, so that the list workspace stays bounded
+    const int ntb_max = kTcMaxCtasPerLaunch / nsplit > 0 ? kTcMaxCtasPerLaunch / nsplit : 1;
+    for (int T0 = 0; T0 < nt; T0 += ntb_max) {
+        const int ntb = nt - T0 < ntb_max ? nt - T0 : ntb_max;
+        tc_sweep_kernel<<<ntb * nsplit, kTcThreads, smem, s>>>(map, b.xr, b.cn, b.ix,
+                                                               reinterpret_cast<const TcScale*>(b.scale), nt, T0, ntb,
+                                                               nsplit, d, b.dr, b.Kp, k, maxn, kth_shared, partial,
+                                                               lists, status);
+        CG_LAUNCH_CHECK();
+    }
 }
 
 }  // namespace culof_gb300
