@@ -75,6 +75,7 @@ _SIGS = {
     "culof_select_knn_tile": ([_P, _P, _P, _I, _I64, _I64, _I, _P, _P, _P], _I),
     "culof_context_knn_device": ([_P, _P, _I64, _I, _I, _I, _P, _P, _P], _I),
     "culof_compute_lrd": ([_P, _P, _P, _P, _I64, _I, _P], _I),
+    "culof_context_lof_backward_device": ([_P, _P, _I64, _I, _I, _I, _P, _P, _P, _P], _I),
     "culof_compute_scores": ([_P, _P, _P, _I64, _I, _P], _I),
     "culof_context_contamination_offset_device": ([_P, _P, _I64, _D, _P], _I),
     "culof_contamination_offset_noalloc": ([_P, _P, _I64, _D, _P], _I),
@@ -277,6 +278,12 @@ class Context:
                    kdist2: int) -> None:
         _check(_lib.culof_context_knn_device(self._h, points, n, d, int(k), int(bool(normalize)), nbr_idx, nbr_d2,
                                              kdist2))
+
+    def lof_backward_device(self, points: int, n: int, d: int, k: int, normalize: bool, nbr_idx: int,
+                            grad_scores: int, grad_points: int, scores_out: int = 0) -> None:
+        """FP64 gradient of sum_i g_i score_i w.r.t. the points, neighbour sets fixed (device pointers)."""
+        _check(_lib.culof_context_lof_backward_device(self._h, points, n, d, int(k), int(bool(normalize)), nbr_idx,
+                                                      grad_scores, grad_points, scores_out or None))
 
     def bf16_gram(self, A: int, rows_a: int, B: int, rows_b: int, K: int, G: int) -> None:
         """G = A B^T on the tensor cores (bf16 in, f32 out; device pointers)."""

@@ -256,6 +256,15 @@ int culof_context_bf16_gram(culof_context* ctx, const void* d_A, int64_t rows_a,
     });
 }
 
+int culof_context_lof_backward_device(culof_context* ctx, const float* d_points, int64_t n_points, int n_dims, int k,
+                                      int normalize, const int32_t* d_nbr_idx, const double* d_grad_scores,
+                                      double* d_grad_points, double* d_scores_out) {
+    return guarded([&] {
+        engine_of(ctx).lof_backward_device(d_points, n_points, n_dims, k, normalize != 0, d_nbr_idx, d_grad_scores,
+                                           d_grad_points, d_scores_out);
+    });
+}
+
 int culof_context_contamination_offset_device(culof_context* ctx, const float* d_nof, int64_t n_points,
                                               double contamination, double* d_offset) {
     return guarded([&] {

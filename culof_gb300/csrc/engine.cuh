@@ -56,6 +56,11 @@ public:
                             double contamination, float* d_nof, int64_t* d_labels, double* d_offset);
     void offset_device(const float* d_nof, int64_t n, double contamination, double* d_offset);
     void bf16_gram(const void* A, int64_t rows_a, const void* B, int64_t rows_b, int K, float* G);
+    // Gradient of sum_i g_i score_i with respect to the points (FP64), the
+    // neighbour sets of a forward k-NN (nbr_idx, k x n) held fixed; optional
+    // FP64 scores of the same fixed-neighbour forward.
+    void lof_backward_device(const float* d_x, int64_t n, int d, int k, bool normalize, const int32_t* nbr_idx,
+                             const double* grad_scores, double* grad_x, double* scores_out);
 
     // Host-pointer forms: copy in, run, copy out, synchronise.
     void lof_host(const float* x, int64_t n, int d, int k, bool normalize, float* scores);
@@ -78,7 +83,7 @@ private:
 
     DevBuf x_, xc_, partial_, mean_, inv_std_, norms_, max_norm_;
     DevBuf nbr_idx_, nbr_d2_, kdist2_, lrd_, scores_, nof_, labels_, offset_, offset_scratch_;
-    DevBuf tile_;
+    DevBuf tile_, bw_;
     // fast path workspaces
     DevBuf morton_, perm_, sort_tmp_, sort_hist_, cols_, rows_, tc_lists_;
     // Device status word of the current call: kernels set it (a bounded wait

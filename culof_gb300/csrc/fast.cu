@@ -708,6 +708,35 @@ void launch_merge(const uint64_t* seed_keys, const uint64_t* partial, const unsi
     CG_LAUNCH_CHECK();
 }
 
+size_t sort_pairs_counts(int64_t n) { return static_cast<size_t>(256) * static_cast<size_t>(ceil_div(n, kSortTile)); }
+
+unsigned* sort_pairs_stable(unsigned* keys, unsigned* vals, unsigned* keys_tmp, unsigned* vals_tmp, int64_t n,
+                            int key_bits, unsigned* counts, cudaStream_t s, unsigned** vals_out) {
+    const int nblocks = static_cast<int>(ceil_div(n, kSortTile));
+    unsigned *kin = keys, *vin = vals, *kout = keys_tmp, *vout = vals_tmp;
+    for (int shift = 0; shift < key_bits; shift += 8) {
+        sort_upsweep_kernel<<<nblocks, kSortThreads, 0, s>>>(kin, n, shift, counts, nblocks);
+        CG_LAUNCH_CHECK();
+        sort_scan_kernel<<<1, 1024, 0, s>>>(counts, static_cast<int64_t>(256) * nblocks);
+        CG_LAUNCH_CHECK();
+        sort_downsweep_kernel<<<nblocks, kSortThreads, 0, s>>>(kin, vin, kout, vout, n, shift, counts, nblocks);
+        CG_LAUNCH_CHECK();
+        unsigned* t = kin;
+        kin = kout;
+        kout = t;
+        t = vin;
+        vin = vout;
+        vout = t;
+    }
+    *vals_out = vin;
+    return kin;
+}
+
+void exclusive_scan_u32(unsigned* data, int64_t len, cudaStream_t s) {
+    sort_scan_kernel<<<1, 1024, 0, s>>>(data, len);
+    CG_LAUNCH_CHECK();
+}
+
 bool fast_path_supported(int64_t n, int d, int k) {
     return d >= 1 && d <= kMaxWideD && k >= 1 && k <= kMaxK && n >= 2 && static_cast<int64_t>(k) < n &&
            n <= (static_cast<int64_t>(1) << 30);

@@ -20,6 +20,16 @@ void wide_seed(const float* tiles, int nt, int d, int k, uint64_t* seed_keys, un
 void wide_sweep(const float* tiles, int nt, int nsplit, int d, int k, const unsigned* maxn,
                 unsigned long long* kth_shared, uint64_t* partial, cudaStream_t s);
 
+// Stable LSD radix sort of (key, value) pairs on the low key_bits bits of the
+// keys (8 bits per pass); keys_tmp / vals_tmp are scratch of n entries and
+// counts holds sort_pairs_counts(n) entries. Returns the buffer holding the
+// sorted keys (keys or keys_tmp) and sets *vals_out to the sorted values.
+size_t sort_pairs_counts(int64_t n);
+unsigned* sort_pairs_stable(unsigned* keys, unsigned* vals, unsigned* keys_tmp, unsigned* vals_tmp, int64_t n,
+                            int key_bits, unsigned* counts, cudaStream_t s, unsigned** vals_out);
+// In-place exclusive prefix sum (one block; for index-sized arrays).
+void exclusive_scan_u32(unsigned* data, int64_t len, cudaStream_t s);
+
 // Shared by the FP32 and tensor-core sweeps (fast.cu).
 int choose_splits(int nt, int sms);
 void launch_merge(const uint64_t* seed_keys, const uint64_t* partial, const unsigned* perm, int64_t n, int nt,

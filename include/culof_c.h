@@ -149,6 +149,21 @@ CULOF_API int culof_compute_lrd(void* cuda_stream, const int32_t* d_nbr_idx, con
 CULOF_API int culof_compute_scores(void* cuda_stream, const int32_t* d_nbr_idx, const float* d_lrd,
                          int64_t n_points, int k, float* d_scores);
 
+/* Sparse LOF backward (no reference counterpart: the reference has no
+ * gradient). Gradient of L = sum_i g_i score_i with respect to the points, the
+ * neighbour sets held fixed: d_nbr_idx is the k x n slot array of a forward
+ * k-NN of the same points (culof_context_knn_device; slot k-1 designates the
+ * k-th neighbour), d_grad_scores n doubles (g), d_grad_points n x d doubles
+ * (row-major, written), d_scores_out n doubles (nullable: the FP64 scores of
+ * the same fixed-neighbour forward). Evaluated in FP64, deterministic (no
+ * floating-point atomics). Requires n_points * k < 2^31. Asynchronous on the
+ * context stream; a neighbour index out of range surfaces as CULOF_ERR_KERNEL
+ * at culof_context_synchronize. */
+CULOF_API int culof_context_lof_backward_device(culof_context* ctx, const float* d_points, int64_t n_points,
+                                                int n_dims, int k, int normalize, const int32_t* d_nbr_idx,
+                                                const double* d_grad_scores, double* d_grad_points,
+                                                double* d_scores_out);
+
 /* The tensor-core building block of the precision form: G = A B^T for
  * row-major bf16 operands A (rows_a x K) and B (rows_b x K), f32 accumulation
  * (tcgen05.mma, TMEM). rows_a and rows_b multiples of 128, K = 128; device
