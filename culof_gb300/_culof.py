@@ -76,6 +76,8 @@ _SIGS = {
     "culof_context_knn_device": ([_P, _P, _I64, _I, _I, _I, _P, _P, _P], _I),
     "culof_compute_lrd": ([_P, _P, _P, _P, _I64, _I, _P], _I),
     "culof_context_lof_backward_device": ([_P, _P, _I64, _I, _I, _I, _P, _P, _P, _P], _I),
+    "culof_context_lof_batched_device": ([_P, _I, _P, _P, _P, _I, _I, _P], _I),
+    "culof_context_set_graphs": ([_P, _I], _I),
     "culof_compute_scores": ([_P, _P, _P, _I64, _I, _P], _I),
     "culof_context_contamination_offset_device": ([_P, _P, _I64, _D, _P], _I),
     "culof_contamination_offset_noalloc": ([_P, _P, _I64, _D, _P], _I),
@@ -278,6 +280,19 @@ class Context:
                    kdist2: int) -> None:
         _check(_lib.culof_context_knn_device(self._h, points, n, d, int(k), int(bool(normalize)), nbr_idx, nbr_d2,
                                              kdist2))
+
+    def lof_batched_device(self, offsets, ks, points: int, d: int, normalize: bool, scores: int) -> None:
+        """LOF scores of many problems in one call (device points/scores,
+        host offsets[num + 1] and ks[num]); graph-replayed when repeated."""
+        off = np.ascontiguousarray(offsets, dtype=np.int64)
+        kk = np.ascontiguousarray(ks, dtype=np.int32)
+        if off.ndim != 1 or kk.ndim != 1 or off.shape[0] != kk.shape[0] + 1:
+            raise ValueError("offsets must have one more entry than ks")
+        _check(_lib.culof_context_lof_batched_device(self._h, int(kk.shape[0]), off.ctypes.data, kk.ctypes.data,
+                                                     points, int(d), int(bool(normalize)), scores))
+
+    def set_graphs(self, on: bool) -> None:
+        _check(_lib.culof_context_set_graphs(self._h, int(bool(on))))
 
     def lof_backward_device(self, points: int, n: int, d: int, k: int, normalize: bool, nbr_idx: int,
                             grad_scores: int, grad_points: int, scores_out: int = 0) -> None:

@@ -256,6 +256,17 @@ int culof_context_bf16_gram(culof_context* ctx, const void* d_A, int64_t rows_a,
     });
 }
 
+int culof_context_lof_batched_device(culof_context* ctx, int num_problems, const int64_t* offsets, const int* ks,
+                                     const float* d_points, int n_dims, int normalize, float* d_scores) {
+    return guarded([&] {
+        engine_of(ctx).lof_batched_device(num_problems, offsets, ks, d_points, n_dims, normalize != 0, d_scores);
+    });
+}
+
+int culof_context_set_graphs(culof_context* ctx, int on) {
+    return guarded([&] { engine_of(ctx).set_graphs(on != 0); });
+}
+
 int culof_context_lof_backward_device(culof_context* ctx, const float* d_points, int64_t n_points, int n_dims, int k,
                                       int normalize, const int32_t* d_nbr_idx, const double* d_grad_scores,
                                       double* d_grad_points, double* d_scores_out) {

@@ -1,0 +1,557 @@
+// Batched LOF over many independent problems in one persistent launch,
+// replayed from a CUDA graph.
+//
+// The reference serves one problem per culof::lof call: a private stream and
+// seven cudaMallocs per call (pipeline.cu:148-168), then the pipeline. A loop
+// of such calls over thousands of small problems is bound by that per-call
+// setup and by launches that cannot fill the GPU. Here one call takes all
+// problems (points concatenated, per-problem offsets and k):
+//   1. batched centring: the single-problem centring's arithmetic, in the
+//      same order (chunks of kCenterChunk rows), for every problem at once;
+//   2. a persistent k-NN kernel: CTAs pull (problem, 128-row tile) work items
+//      from an atomic counter, largest problems first, and select each row's
+//      exact k nearest among its problem's points (FP32 direct differences,
+//      the oracle's formula, two rows per packed f32x2 instruction) into
+//      per-row lists in shared memory;
+//   3. batched lrd and scores with the reference's FP64 sums.
+// Every problem's scores are bit-identical to a single-problem call. The
+// launch sequence of a given batch layout is captured once as a CUDA graph
+// and replayed; on first sight of a layout a small autotuner times the k-NN
+// kernel's variants (CTAs per SM, packed or scalar arithmetic) and keeps the
+// fastest.
+#include <algorithm>
+#include <cstring>
+#include <sstream>
+#include <vector>
+
+#include "common.cuh"
+#include "engine.cuh"
+#include "sweep_common.cuh"
+
+namespace culof_gb300 {
+
+namespace {
+
+using namespace sweep;
+
+constexpr int kBM = 80;          // list capacity per row: k + 32 free slots (two CTAs per SM)
+constexpr int kBMaxK = kBM - 32;
+constexpr int kBMaxD = 64;
+
+// ---- batched centring (prep.cu's arithmetic per problem) -------------------
+
+// One thread per (global chunk, feature); chunk g belongs to problem cp[g].
+__global__ void bc_partials_kernel(const float* __restrict__ x, const int64_t* __restrict__ off, int d,
+                                   const int* __restrict__ cp, const int64_t* __restrict__ coff, int64_t nchunks,
+                                   const double* __restrict__ mean, double* __restrict__ partial) {
+    const int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (t >= nchunks * d) return;
+    const int64_t g = t / d;
+    const int f = static_cast<int>(t % d);
+    const int p = cp[g];
+    const int64_t c = g - coff[p];
+    const int64_t n = off[p + 1] - off[p];
+    const float* xp = x + off[p] * d;
+    const int64_t begin = c * kCenterChunk;
+    const int64_t end = begin + kCenterChunk < n ? begin + kCenterChunk : n;
+    double s = 0.0;
+    if (mean == nullptr) {
+        for (int64_t i = begin; i < end; ++i) s = __dadd_rn(s, static_cast<double>(xp[i * d + f]));
+    } else {
+        const double m = mean[static_cast<int64_t>(p) * d + f];
+        for (int64_t i = begin; i < end; ++i) {
+            const double v = __dsub_rn(static_cast<double>(xp[i * d + f]), m);
+            s = __dadd_rn(s, __dmul_rn(v, v));
+        }
+    }
+    partial[t] = s;
+}
+
+__global__ void bc_finalize_kernel(const double* __restrict__ partial, const int64_t* __restrict__ off,
+                                   const int64_t* __restrict__ coff, int num, int d, int mode,
+                                   double* __restrict__ mean, double* __restrict__ inv_std) {
+    const int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (t >= static_cast<int64_t>(num) * d) return;
+    const int p = static_cast<int>(t / d);
+    const int f = static_cast<int>(t % d);
+    double total = 0.0;
+    for (int64_t c = coff[p]; c < coff[p + 1]; ++c) total = __dadd_rn(total, partial[c * d + f]);
+    const double dn = static_cast<double>(off[p + 1] - off[p]);
+    if (mode == 0) {
+        mean[t] = __ddiv_rn(total, dn);
+        inv_std[t] = 1.0;
+    } else {
+        const double sd = __dsqrt_rn(__ddiv_rn(total, dn));
+        inv_std[t] = (sd > 1e-12) ? __ddiv_rn(1.0, sd) : 1.0;
+    }
+}
+
+__global__ void bc_apply_kernel(const float* __restrict__ x, int64_t ntot, int d, const int* __restrict__ pid,
+                                const double* __restrict__ mean, const double* __restrict__ inv_std,
+                                float* __restrict__ xc) {
+    for (int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; t < ntot * d;
+         t += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const int64_t i = t / d;
+        const int f = static_cast<int>(t % d);
+        const int64_t pf = static_cast<int64_t>(pid[i]) * d + f;
+        xc[t] = __double2float_rn(__dmul_rn(__dsub_rn(static_cast<double>(x[t]), mean[pf]), inv_std[pf]));
+    }
+}
+
+// ---- persistent k-NN ---------------------------------------------------------
+
+template <int DP>
+struct BatchSmem {
+    RowLists<kBM> L;
+    float rows[kRT][DP + 1];  // this item's rows (odd stride)
+    float cols[kCT][DP + 1];  // one column tile
+    int item;
+};
+
+// Exact squared distance chain of rows (r, r + 1) against one column (lane's),
+// both written into s0, s1 (the oracle's formula, bit for bit).
+template <int DP, bool PACKED>
+__device__ __forceinline__ void dist_pair(const BatchSmem<DP>& sh, int r, const float (&col)[DP], int d, float& s0,
+                                          float& s1) {
+    if constexpr (PACKED) {
+        uint64_t s2 = 0;
+#pragma unroll
+        for (int f = 0; f < DP; ++f) {
+            if (f < d) {
+                const uint64_t a2 = (static_cast<uint64_t>(__float_as_uint(sh.rows[r + 1][f])) << 32) |
+                                    __float_as_uint(sh.rows[r][f]);
+                uint64_t t2;
+                asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(t2) : "l"(a2), "l"(dup2(col[f])));
+                s2 = fma2(t2, t2, s2);
+            }
+        }
+        s0 = lo_f(s2);
+        s1 = hi_f(s2);
+    } else {
+        float a = 0.0f, b = 0.0f;
+#pragma unroll
+        for (int f = 0; f < DP; ++f) {
+            if (f < d) {
+                const float t0 = __fsub_rn(sh.rows[r][f], col[f]);
+                const float t1 = __fsub_rn(sh.rows[r + 1][f], col[f]);
+                a = __fmaf_rn(t0, t0, a);
+                b = __fmaf_rn(t1, t1, b);
+            }
+        }
+        s0 = a;
+        s1 = b;
+    }
+}
+
+// Append this lane's key for row r (if it beats the row's k-th key), keeping
+// 32 free slots: warp-uniform.
+__device__ __forceinline__ void offer(RowLists<kBM>& L, int r, uint64_t key, int k) {
+    const int lane = threadIdx.x & 31;
+    bool pass = key < L.kth[r];
+    unsigned m = __ballot_sync(0xffffffffu, pass);
+    if (!m) return;
+    if (L.cnt[r] > kBM - 32) {
+        compact_row<kBM>(L, r, k, 0.0f, 8);
+        pass = key < L.kth[r];
+        m = __ballot_sync(0xffffffffu, pass);
+        if (!m) return;
+    }
+    const int c = L.cnt[r];
+    if (pass) L.list[r][c + __popc(m & ((1u << lane) - 1u))] = key;
+    __syncwarp();
+    if (lane == 0) L.cnt[r] = c + __popc(m);
+    __syncwarp();
+}
+
+template <int DP, bool PACKED>
+__global__ void __launch_bounds__(kThreads)
+batched_knn_kernel(const float* __restrict__ xc, const int64_t* __restrict__ off, const int* __restrict__ ks,
+                   const int64_t* __restrict__ nkoff, const uint2* __restrict__ items, int nitems, int d,
+                   unsigned* __restrict__ counter, int32_t* __restrict__ nbr_idx, float* __restrict__ nbr_d2,
+                   float* __restrict__ kdist2) {
+    extern __shared__ __align__(16) unsigned char braw[];
+    BatchSmem<DP>& sh = *reinterpret_cast<BatchSmem<DP>*>(braw);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (;;) {
+        if (tid == 0) sh.item = static_cast<int>(atomicAdd(counter, 1u));
+        __syncthreads();
+        const int item = sh.item;
+        if (item >= nitems) break;
+        const int p = static_cast<int>(items[item].x);
+        const int T = static_cast<int>(items[item].y);
+        const int64_t base = off[p];
+        const int n = static_cast<int>(off[p + 1] - base);
+        const int k = ks[p];
+        const float* xp = xc + base * d;
+        const int r0 = T * kRT;
+        for (int i = tid; i < kRT * DP; i += kThreads) {
+            const int r = i / DP, f = i % DP;
+            sh.rows[r][f] = (r0 + r < n && f < d) ? xp[static_cast<int64_t>(r0 + r) * d + f] : 0.0f;
+        }
+        if (tid < kRT) {
+            sh.L.cnt[tid] = 0;
+            sh.L.kth[tid] = kKeyMax;
+            sh.L.row_norm[tid] = 0.0f;
+        }
+        __syncthreads();
+        for (int c0 = 0; c0 < n; c0 += kCT) {
+            for (int i = tid; i < kCT * DP; i += kThreads) {
+                const int c = i / DP, f = i % DP;
+                sh.cols[c][f] = (c0 + c < n && f < d) ? xp[static_cast<int64_t>(c0 + c) * d + f] : 0.0f;
+            }
+            __syncthreads();
+#pragma unroll 1
+            for (int sub = 0; sub < kCT / 32; ++sub) {
+                const int c = sub * 32 + lane;
+                const int gc = c0 + c;
+                float col[DP];
+#pragma unroll
+                for (int f = 0; f < DP; ++f) col[f] = sh.cols[c][f];
+#pragma unroll 1
+                for (int rr = 0; rr < kRowsPerWarp; rr += 2) {
+                    const int r = warp * kRowsPerWarp + rr;
+                    if (r0 + r >= n) break;  // warp-uniform: rows beyond the problem
+                    float s0, s1;
+                    dist_pair<DP, PACKED>(sh, r, col, d, s0, s1);
+                    const bool ok0 = gc < n && gc != r0 + r;
+                    const bool ok1 = gc < n && gc != r0 + r + 1 && r0 + r + 1 < n;
+                    offer(sh.L, r, ok0 ? make_key(__float_as_uint(s0), static_cast<uint32_t>(gc)) : kKeyMax, k);
+                    offer(sh.L, r + 1, ok1 ? make_key(__float_as_uint(s1), static_cast<uint32_t>(gc)) : kKeyMax, k);
+                }
+            }
+            __syncthreads();
+        }
+        // the k best per row, written in the reference's slot order
+        for (int rr = 0; rr < kRowsPerWarp; ++rr) {
+            const int r = warp * kRowsPerWarp + rr;
+            const int il = r0 + r;
+            if (il >= n) break;
+            compact_row<kBM>(sh.L, r, k, 0.0f, 8);
+            const uint64_t kth = sh.L.list[r][k - 1];
+            const uint32_t kbits = key_bits(kth);
+            int below = 0;
+            for (int e = lane; e < k; e += 32) below += key_bits(sh.L.list[r][e]) < kbits ? 1 : 0;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) below += __shfl_xor_sync(0xffffffffu, below, o);
+            int32_t* oi = nbr_idx + nkoff[p];
+            float* od = nbr_d2 + nkoff[p];
+            for (int e = lane; e < k; e += 32) {
+                const uint64_t y = sh.L.list[r][e];
+                int slot = e;
+                if (e < below) {
+                    const uint32_t yi = key_index(y);
+                    slot = 0;
+                    for (int q = 0; q < below; ++q) slot += key_index(sh.L.list[r][q]) < yi ? 1 : 0;
+                }
+                oi[static_cast<int64_t>(slot) * n + il] = static_cast<int32_t>(key_index(y));
+                od[static_cast<int64_t>(slot) * n + il] = __uint_as_float(key_bits(y));
+            }
+            if (lane == 0) kdist2[base + il] = __uint_as_float(kbits);
+        }
+        __syncthreads();
+    }
+}
+
+// ---- batched lrd and scores (lof.cu's arithmetic, local indices) -------------
+
+__global__ void bl_lrd_kernel(int64_t ntot, const int* __restrict__ pid, const int64_t* __restrict__ off,
+                              const int* __restrict__ ks, const int64_t* __restrict__ nkoff,
+                              const int32_t* __restrict__ nbr_idx, const float* __restrict__ nbr_d2,
+                              const float* __restrict__ kdist2, float* __restrict__ lrd) {
+    const int64_t g = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (g >= ntot) return;
+    const int p = pid[g];
+    const int64_t base = off[p];
+    const int64_t n = off[p + 1] - base, i = g - base;
+    const int k = ks[p];
+    const int32_t* ni = nbr_idx + nkoff[p];
+    const float* nd = nbr_d2 + nkoff[p];
+    double sum = 0.0;
+    for (int t = 0; t < k; ++t) {
+        const int64_t o = static_cast<int64_t>(t) * n + i;
+        const int32_t j = ni[o];
+        const float kj = (j >= 0 && j < n) ? kdist2[base + j] : __int_as_float(0x7fc00000);
+        sum = __dadd_rn(sum, __dsqrt_rn(static_cast<double>(fmaxf(kj, nd[o]))));
+    }
+    lrd[g] = __double2float_rn(__ddiv_rn(1.0, __dadd_rn(__ddiv_rn(sum, static_cast<double>(k)), 1e-10)));
+}
+
+__global__ void bl_score_kernel(int64_t ntot, const int* __restrict__ pid, const int64_t* __restrict__ off,
+                                const int* __restrict__ ks, const int64_t* __restrict__ nkoff,
+                                const int32_t* __restrict__ nbr_idx, const float* __restrict__ lrd,
+                                float* __restrict__ scores) {
+    const int64_t g = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (g >= ntot) return;
+    const int p = pid[g];
+    const int64_t base = off[p];
+    const int64_t n = off[p + 1] - base, i = g - base;
+    const int k = ks[p];
+    const int32_t* ni = nbr_idx + nkoff[p];
+    const double self = static_cast<double>(lrd[g]);
+    double sum = 0.0;
+    for (int t = 0; t < k; ++t) {
+        const int32_t j = ni[static_cast<int64_t>(t) * n + i];
+        const double lj = (j >= 0 && j < n) ? static_cast<double>(lrd[base + j]) : __longlong_as_double(0x7ff8000000000000ll);
+        sum = __dadd_rn(sum, __ddiv_rn(lj, self));
+    }
+    scores[g] = __double2float_rn(__ddiv_rn(sum, static_cast<double>(k)));
+}
+
+__global__ void pid_kernel(const int64_t* __restrict__ off, int num, int* __restrict__ pid) {
+    // one block per problem
+    for (int p = blockIdx.x; p < num; p += gridDim.x)
+        for (int64_t i = off[p] + threadIdx.x; i < off[p + 1]; i += blockDim.x) pid[i] = p;
+}
+
+int dp_for(int d) { return d <= 4 ? 4 : d <= 8 ? 8 : d <= 16 ? 16 : d <= 32 ? 32 : 64; }
+
+template <int DP, bool PACKED>
+void launch_knn_t(int grid, const BatchDev& b, cudaStream_t s) {
+    const size_t smem = sizeof(BatchSmem<DP>);
+    static bool configured = false;
+    if (!configured) {
+        CG_CUDA(cudaFuncSetAttribute(batched_knn_kernel<DP, PACKED>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     static_cast<int>(smem)));
+        configured = true;
+    }
+    batched_knn_kernel<DP, PACKED><<<grid, kThreads, smem, s>>>(b.xc, b.off, b.ks, b.nkoff, b.items, b.nitems, b.d,
+                                                               b.counter, b.nbr, b.d2, b.kd);
+    CG_LAUNCH_CHECK();
+}
+
+void launch_knn(int dp, bool packed, int grid, const BatchDev& b, cudaStream_t s) {
+#define CG_B(DPV)                                                    \
+    case DPV:                                                        \
+        if (packed && DPV <= 32) launch_knn_t<DPV, true>(grid, b, s); \
+        else launch_knn_t<DPV, false>(grid, b, s);                   \
+        break;
+    switch (dp) {
+        CG_B(4)
+        CG_B(8)
+        CG_B(16)
+        CG_B(32)
+        CG_B(64)
+        default: throw Error(kInternal, "bad padded dimension");
+    }
+#undef CG_B
+}
+
+template <int DP>
+size_t knn_smem() { return sizeof(BatchSmem<DP>); }
+size_t knn_smem_for(int dp) {
+    switch (dp) {
+        case 4: return knn_smem<4>();
+        case 8: return knn_smem<8>();
+        case 16: return knn_smem<16>();
+        case 32: return knn_smem<32>();
+        default: return knn_smem<64>();
+    }
+}
+
+int grid_cap(int64_t items) {
+    int64_t g = ceil_div(items, 256);
+    if (g > 152 * 16) g = 152 * 16;
+    return static_cast<int>(g < 1 ? 1 : g);
+}
+
+}  // namespace
+
+// ---- host orchestration --------------------------------------------------------
+
+void Engine::batch_plan(int num, const int64_t* offsets, const int* ks, int d, bool normalize) {
+    if (num < 1) throw Error(kInvalidArgument, "num_problems must be >= 1");
+    if (!offsets || !ks) throw Error(kInvalidArgument, "offsets and ks must not be null");
+    if (d < 1 || d > kBMaxD) throw Error(kInvalidArgument, "the batched path takes 1 <= n_dims <= 64");
+    if (offsets[0] != 0) throw Error(kInvalidArgument, "offsets[0] must be 0");
+    BatchPlan& P = bplan_;
+    P.num = num;
+    P.d = d;
+    P.normalize = normalize;
+    P.off.assign(offsets, offsets + num + 1);
+    P.ks.assign(ks, ks + num);
+    P.nkoff.assign(num + 1, 0);
+    P.coff.assign(num + 1, 0);
+    std::vector<std::pair<int64_t, uint2>> items;
+    std::vector<int> cp;
+    for (int p = 0; p < num; ++p) {
+        const int64_t n = offsets[p + 1] - offsets[p];
+        const int k = ks[p];
+        if (n < 2 || n > 0x7FFFFFFFll) {
+            std::ostringstream os;
+            os << "problem " << p << ": n_points must be >= 2 (got " << n << ")";
+            throw Error(kInvalidArgument, os.str());
+        }
+        if (k < 1 || k >= n || k > kBMaxK) {
+            std::ostringstream os;
+            os << "problem " << p << ": k must satisfy 1 <= k <= n_points - 1 and k <= " << kBMaxK << " (got k=" << k
+               << ", n_points=" << n << ")";
+            throw Error(kInvalidArgument, os.str());
+        }
+        P.nkoff[p + 1] = P.nkoff[p] + n * k;
+        const int64_t chunks = ceil_div(n, kCenterChunk);
+        P.coff[p + 1] = P.coff[p] + chunks;
+        for (int64_t c = 0; c < chunks; ++c) cp.push_back(p);
+        const int64_t tiles = ceil_div(n, kRT);
+        for (int64_t t = 0; t < tiles; ++t)
+            items.push_back({n, make_uint2(static_cast<unsigned>(p), static_cast<unsigned>(t))});
+    }
+    // largest problems first: their items are the longest, the tail stays short
+    std::stable_sort(items.begin(), items.end(),
+                     [](const std::pair<int64_t, uint2>& a, const std::pair<int64_t, uint2>& b) { return a.first > b.first; });
+    P.items.resize(items.size());
+    for (size_t i = 0; i < items.size(); ++i) P.items[i] = items[i].second;
+    P.ntot = offsets[num];
+    P.nchunks = P.coff[num];
+    // device copies of the plan (synchronous, before any capture)
+    cudaStream_t s = stream_;
+    BatchDev& b = bdev_;
+    b.off = bplan_off_.as<int64_t>(num + 1);
+    b.nkoff = bplan_nkoff_.as<int64_t>(num + 1);
+    b.coff = bplan_coff_.as<int64_t>(num + 1);
+    b.ks = bplan_ks_.as<int>(num);
+    b.items = bplan_items_.as<uint2>(P.items.size());
+    b.cp = bplan_cp_.as<int>(cp.size() ? cp.size() : 1);
+    CG_CUDA(cudaMemcpyAsync(b.off, P.off.data(), sizeof(int64_t) * (num + 1), cudaMemcpyHostToDevice, s));
+    CG_CUDA(cudaMemcpyAsync(b.nkoff, P.nkoff.data(), sizeof(int64_t) * (num + 1), cudaMemcpyHostToDevice, s));
+    CG_CUDA(cudaMemcpyAsync(b.coff, P.coff.data(), sizeof(int64_t) * (num + 1), cudaMemcpyHostToDevice, s));
+    CG_CUDA(cudaMemcpyAsync(b.ks, P.ks.data(), sizeof(int) * num, cudaMemcpyHostToDevice, s));
+    CG_CUDA(cudaMemcpyAsync(b.items, P.items.data(), sizeof(uint2) * P.items.size(), cudaMemcpyHostToDevice, s));
+    CG_CUDA(cudaMemcpyAsync(b.cp, cp.data(), sizeof(int) * cp.size(), cudaMemcpyHostToDevice, s));
+    b.nitems = static_cast<int>(P.items.size());
+    b.d = d;
+    // workspaces
+    b.pid = bpid_.as<int>(P.ntot);
+    b.xc = bxc_.as<float>(static_cast<size_t>(P.ntot) * d);
+    b.partial = bpartial_.as<double>(static_cast<size_t>(P.nchunks) * d);
+    b.mean = bmean_.as<double>(static_cast<size_t>(num) * d);
+    b.inv = binv_.as<double>(static_cast<size_t>(num) * d);
+    b.nbr = bnbr_.as<int32_t>(P.nkoff[num]);
+    b.d2 = bd2_.as<float>(P.nkoff[num]);
+    b.kd = bkd_.as<float>(P.ntot);
+    b.lrd = blrd_.as<float>(P.ntot);
+    b.counter = bcounter_.as<unsigned>(1);
+    pid_kernel<<<num < 4096 ? num : 4096, 256, 0, s>>>(b.off, num, b.pid);
+    CG_LAUNCH_CHECK();
+    CG_CUDA(cudaStreamSynchronize(s));
+    bgraph_valid_ = false;
+    btuned_ = false;
+}
+
+void Engine::batch_launch(const float* d_x, float* d_scores) {
+    const BatchPlan& P = bplan_;
+    BatchDev& b = bdev_;
+    cudaStream_t s = stream_;
+    const int d = P.d;
+    const int64_t cd = P.nchunks * d;
+    bc_partials_kernel<<<static_cast<unsigned>(ceil_div(cd, 256)), 256, 0, s>>>(d_x, b.off, d, b.cp, b.coff,
+                                                                                 P.nchunks, nullptr, b.partial);
+    CG_LAUNCH_CHECK();
+    bc_finalize_kernel<<<static_cast<unsigned>(ceil_div(static_cast<int64_t>(P.num) * d, 128)), 128, 0, s>>>(
+        b.partial, b.off, b.coff, P.num, d, 0, b.mean, b.inv);
+    CG_LAUNCH_CHECK();
+    if (P.normalize) {
+        bc_partials_kernel<<<static_cast<unsigned>(ceil_div(cd, 256)), 256, 0, s>>>(d_x, b.off, d, b.cp, b.coff,
+                                                                                     P.nchunks, b.mean, b.partial);
+        CG_LAUNCH_CHECK();
+        bc_finalize_kernel<<<static_cast<unsigned>(ceil_div(static_cast<int64_t>(P.num) * d, 128)), 128, 0, s>>>(
+            b.partial, b.off, b.coff, P.num, d, 1, b.mean, b.inv);
+        CG_LAUNCH_CHECK();
+    }
+    bc_apply_kernel<<<grid_cap(P.ntot * d), 256, 0, s>>>(d_x, P.ntot, d, b.pid, b.mean, b.inv, b.xc);
+    CG_LAUNCH_CHECK();
+    CG_CUDA(cudaMemsetAsync(b.counter, 0, sizeof(unsigned), s));
+    launch_knn(dp_for(d), btune_packed_, btune_grid_, b, s);
+    bl_lrd_kernel<<<static_cast<unsigned>(ceil_div(P.ntot, 256)), 256, 0, s>>>(P.ntot, b.pid, b.off, b.ks, b.nkoff,
+                                                                               b.nbr, b.d2, b.kd, b.lrd);
+    CG_LAUNCH_CHECK();
+    bl_score_kernel<<<static_cast<unsigned>(ceil_div(P.ntot, 256)), 256, 0, s>>>(P.ntot, b.pid, b.off, b.ks,
+                                                                                 b.nkoff, b.nbr, b.lrd, d_scores);
+    CG_LAUNCH_CHECK();
+}
+
+// Time the k-NN kernel's variants on this batch (once per layout).
+void Engine::batch_autotune(const float* d_x, float* d_scores) {
+    int sms = 152;
+    CG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_));
+    const int dp = dp_for(bplan_.d);
+    const size_t smem = knn_smem_for(dp);
+    int max_per_sm = static_cast<int>(227 * 1024 / (smem + 1024));
+    if (max_per_sm < 1) max_per_sm = 1;
+    if (max_per_sm > 2) max_per_sm = 2;
+    cudaEvent_t e0, e1;
+    CG_CUDA(cudaEventCreate(&e0));
+    CG_CUDA(cudaEventCreate(&e1));
+    float best = 1e30f;
+    for (int per = 1; per <= max_per_sm; ++per) {
+        for (int packed = 0; packed <= (dp <= 32 ? 1 : 0); ++packed) {
+            btune_grid_ = per * sms;
+            btune_packed_ = packed != 0;
+            batch_launch(d_x, d_scores);  // warm (first use configures the kernel)
+            CG_CUDA(cudaEventRecord(e0, stream_));
+            batch_launch(d_x, d_scores);
+            CG_CUDA(cudaEventRecord(e1, stream_));
+            CG_CUDA(cudaEventSynchronize(e1));
+            float ms = 0.0f;
+            CG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            if (ms < best) {
+                best = ms;
+                bbest_grid_ = btune_grid_;
+                bbest_packed_ = btune_packed_;
+            }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    btune_grid_ = bbest_grid_;
+    btune_packed_ = bbest_packed_;
+    btuned_ = true;
+}
+
+bool Engine::batch_same_plan(int num, const int64_t* offsets, const int* ks, int d, bool normalize) const {
+    const BatchPlan& P = bplan_;
+    if (P.num != num || P.d != d || P.normalize != normalize) return false;
+    if (std::memcmp(P.off.data(), offsets, sizeof(int64_t) * (num + 1)) != 0) return false;
+    return std::memcmp(P.ks.data(), ks, sizeof(int) * num) == 0;
+}
+
+void Engine::lof_batched_device(int num, const int64_t* offsets, const int* ks, const float* d_x, int d,
+                                bool normalize, float* d_scores) {
+    if (!d_x || !d_scores) throw Error(kInvalidArgument, "device pointers must not be null");
+    CG_CUDA(cudaSetDevice(device_));
+    if (!(bplan_.num > 0 && batch_same_plan(num, offsets, ks, d, normalize))) batch_plan(num, offsets, ks, d, normalize);
+    if (!btuned_) batch_autotune(d_x, d_scores);
+    if (!use_graphs_) {
+        batch_launch(d_x, d_scores);
+        return;
+    }
+    if (!bgraph_valid_ || bgraph_x_ != d_x || bgraph_scores_ != d_scores || bgraph_stream_ != stream_) {
+        if (bgraph_exec_) {
+            cudaGraphExecDestroy(bgraph_exec_);
+            bgraph_exec_ = nullptr;
+        }
+        cudaGraph_t g = nullptr;
+        const unsigned long long before = launch_count();
+        CG_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+        try {
+            batch_launch(d_x, d_scores);
+        } catch (...) {
+            cudaStreamEndCapture(stream_, &g);
+            if (g) cudaGraphDestroy(g);
+            throw;
+        }
+        CG_CUDA(cudaStreamEndCapture(stream_, &g));
+        bgraph_kernels_ = launch_count() - before;  // captured, not launched
+        uncount_launches(bgraph_kernels_);
+        const cudaError_t ie = cudaGraphInstantiate(&bgraph_exec_, g, 0);
+        cudaGraphDestroy(g);
+        CG_CUDA(ie);
+        bgraph_valid_ = true;
+        bgraph_x_ = d_x;
+        bgraph_scores_ = d_scores;
+        bgraph_stream_ = stream_;
+    }
+    CG_CUDA(cudaGraphLaunch(bgraph_exec_, stream_));
+    count_launches(bgraph_kernels_);
+}
+
+}  // namespace culof_gb300

@@ -36,6 +36,8 @@ void throw_cuda(cudaError_t err, const char* file, int line, const char* expr);
 // Every kernel launch of the library is followed by this check, which also
 // counts the launch (culof_kernel_launch_count in the C ABI).
 void count_launch();
+void count_launches(unsigned long long n);
+void uncount_launches(unsigned long long n);
 #define CG_LAUNCH_CHECK()                  \
     do {                                   \
         ::culof_gb300::count_launch();     \

@@ -17,6 +17,8 @@ std::atomic<unsigned long long> g_launches{0};
 }
 
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+void count_launches(unsigned long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+void uncount_launches(unsigned long long n) { g_launches.fetch_sub(n, std::memory_order_relaxed); }
 unsigned long long launch_count() { return g_launches.load(std::memory_order_relaxed); }
 
 void throw_cuda(cudaError_t err, const char* file, int line, const char* expr) {
@@ -74,6 +76,7 @@ Engine::Engine(int device) : device_(device) {
 }
 
 Engine::~Engine() {
+    if (bgraph_exec_) cudaGraphExecDestroy(bgraph_exec_);
     for (auto& e : events_)
         if (e) cudaEventDestroy(e);
     if (own_stream_) {

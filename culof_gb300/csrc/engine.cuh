@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <vector>
+
 #include "common.cuh"
 #include "prep.cuh"
 
@@ -28,6 +30,30 @@ public:
 private:
     void* ptr_ = nullptr;
     size_t cap_ = 0;
+};
+
+// A batch of independent problems (batched.cu): host plan and device copies.
+struct BatchPlan {
+    int num = 0;
+    int d = 0;
+    bool normalize = false;
+    std::vector<int64_t> off, nkoff, coff;  // points, k-NN slots, centring chunks per problem (prefix sums)
+    std::vector<int> ks;
+    std::vector<uint2> items;  // (problem, row tile), largest problems first
+    int64_t ntot = 0, nchunks = 0;
+};
+struct BatchDev {
+    int64_t *off = nullptr, *nkoff = nullptr, *coff = nullptr;
+    int* ks = nullptr;
+    uint2* items = nullptr;
+    int* cp = nullptr;  // problem of each centring chunk
+    int nitems = 0, d = 0;
+    int* pid = nullptr;  // problem of each point
+    float* xc = nullptr;
+    double *partial = nullptr, *mean = nullptr, *inv = nullptr;
+    int32_t* nbr = nullptr;
+    float *d2 = nullptr, *kd = nullptr, *lrd = nullptr;
+    unsigned* counter = nullptr;
 };
 
 enum Path : int { kPathAuto = 0, kPathFast = 1, kPathGeneral = 2, kPathTensor = 3 };
@@ -59,6 +85,12 @@ public:
     // Gradient of sum_i g_i score_i with respect to the points (FP64), the
     // neighbour sets of a forward k-NN (nbr_idx, k x n) held fixed; optional
     // FP64 scores of the same fixed-neighbour forward.
+    // LOF scores of many independent problems (points concatenated; host
+    // offsets[num + 1], ks[num]) in one persistent launch, replayed from a
+    // CUDA graph while the batch layout and pointers repeat.
+    void lof_batched_device(int num, const int64_t* offsets, const int* ks, const float* d_x, int d, bool normalize,
+                            float* d_scores);
+    void set_graphs(bool on) { use_graphs_ = on; }
     void lof_backward_device(const float* d_x, int64_t n, int d, int k, bool normalize, const int32_t* nbr_idx,
                              const double* grad_scores, double* grad_x, double* scores_out);
 
@@ -68,6 +100,10 @@ public:
                           double contamination, float* nof, int64_t* labels, double* offset);
 
 private:
+    void batch_plan(int num, const int64_t* offsets, const int* ks, int d, bool normalize);
+    bool batch_same_plan(int num, const int64_t* offsets, const int* ks, int d, bool normalize) const;
+    void batch_launch(const float* d_x, float* d_scores);
+    void batch_autotune(const float* d_x, float* d_scores);
     int choose_path(int64_t n, int d, int k) const;
     void knn_general(const float* xc, const float* norms, int64_t n, int d, int k, int32_t* nbr_idx,
                      float* nbr_d2, float* kdist2);
@@ -84,6 +120,20 @@ private:
     DevBuf x_, xc_, partial_, mean_, inv_std_, norms_, max_norm_;
     DevBuf nbr_idx_, nbr_d2_, kdist2_, lrd_, scores_, nof_, labels_, offset_, offset_scratch_;
     DevBuf tile_, bw_;
+    // batched path (batched.cu)
+    BatchPlan bplan_;
+    BatchDev bdev_;
+    DevBuf bplan_off_, bplan_nkoff_, bplan_coff_, bplan_ks_, bplan_items_, bplan_cp_;
+    DevBuf bpid_, bxc_, bpartial_, bmean_, binv_, bnbr_, bd2_, bkd_, blrd_, bcounter_;
+    bool use_graphs_ = true;
+    bool btuned_ = false, btune_packed_ = true, bbest_packed_ = true;
+    int btune_grid_ = 152, bbest_grid_ = 152;
+    cudaGraphExec_t bgraph_exec_ = nullptr;
+    bool bgraph_valid_ = false;
+    const float* bgraph_x_ = nullptr;
+    float* bgraph_scores_ = nullptr;
+    cudaStream_t bgraph_stream_ = nullptr;
+    unsigned long long bgraph_kernels_ = 0;
     // fast path workspaces
     DevBuf morton_, perm_, sort_tmp_, sort_hist_, cols_, rows_, tc_lists_;
     // Device status word of the current call: kernels set it (a bounded wait

@@ -127,8 +127,11 @@ struct RowLists {
 // smallest; tighten the row's k-th key (only downwards) and its threshold.
 template <int M>
 __device__ void compact_row(RowLists<M>& L, int r, int k, float nmax, int dp) {
-    // the bitonic network needs a power of two: pad M/32 registers up (with kKeyMax)
-    constexpr int E = (M / 32) <= 1 ? 1 : (M / 32) <= 2 ? 2 : (M / 32) <= 4 ? 4 : 8;
+    // the bitonic network needs a power of two: ceil(M / 32) registers per
+    // lane, padded up to one (with kKeyMax)
+    constexpr int R = (M + 31) / 32;
+    constexpr int E = R <= 1 ? 1 : R <= 2 ? 2 : R <= 4 ? 4 : 8;
+    static_assert(32 * E >= M, "the sort covers the whole list");
     static_assert(M % 8 == 0 && M <= 256, "list capacity");
     const int lane = threadIdx.x & 31;
     const int c = min(L.cnt[r], M);

@@ -149,6 +149,25 @@ CULOF_API int culof_compute_lrd(void* cuda_stream, const int32_t* d_nbr_idx, con
 CULOF_API int culof_compute_scores(void* cuda_stream, const int32_t* d_nbr_idx, const float* d_lrd,
                          int64_t n_points, int k, float* d_scores);
 
+/* Batched LOF (no reference counterpart: the reference serves one problem
+ * per culof::lof call, pipeline.cu:131-207). Positive LOF scores of
+ * num_problems independent problems in one call: d_points holds every
+ * problem's points concatenated (row-major float32, n_dims columns, device),
+ * offsets (host, num_problems + 1 entries, offsets[0] = 0) delimits them and
+ * ks (host) gives each problem's k; d_scores (device, offsets[num_problems]
+ * floats) receives the scores in the same order. Each problem obeys the
+ * reference's rules (n >= 2, 1 <= k < n) and the batched limits k <= 48,
+ * n_dims <= 64. Every problem's scores are bit-identical to a single-problem
+ * culof_context_lof call. The first call with a batch layout plans it and
+ * times the kernel variants; the launch sequence is then captured as a CUDA
+ * graph and replayed while the layout, the two pointers and the stream stay
+ * the same. Asynchronous on the context stream. */
+CULOF_API int culof_context_lof_batched_device(culof_context* ctx, int num_problems, const int64_t* offsets,
+                                               const int* ks, const float* d_points, int n_dims, int normalize,
+                                               float* d_scores);
+/* Graph capture of repeated batched calls: on (1, default) or off (0). */
+CULOF_API int culof_context_set_graphs(culof_context* ctx, int on);
+
 /* Sparse LOF backward (no reference counterpart: the reference has no
  * gradient). Gradient of L = sum_i g_i score_i with respect to the points, the
  * neighbour sets held fixed: d_nbr_idx is the k x n slot array of a forward
