@@ -11,14 +11,14 @@
 //   2. a persistent k-NN kernel: CTAs pull (problem, 128-row tile) work items
 //      from an atomic counter, largest problems first, and select each row's
 //      exact k nearest among its problem's points (FP32 direct differences,
-//      the oracle's formula, two rows per packed f32x2 instruction) into
+//      the oracle's formula, two columns per packed f32x2 instruction) into
 //      per-row lists in shared memory;
 //   3. batched lrd and scores with the reference's FP64 sums.
 // Every problem's scores are bit-identical to a single-problem call. The
 // launch sequence of a given batch layout is captured once as a CUDA graph
 // and replayed; on first sight of a layout a small autotuner times the k-NN
-// kernel's variants (CTAs per SM, packed or scalar arithmetic) and keeps the
-// fastest.
+// kernel's variants (CTAs per SM, one or two column pairs per lane) and
+// keeps the fastest.
 #include <algorithm>
 #include <cstring>
 #include <sstream>
@@ -103,45 +103,10 @@ __global__ void bc_apply_kernel(const float* __restrict__ x, int64_t ntot, int d
 template <int DP>
 struct BatchSmem {
     RowLists<kBM> L;
-    float rows[kRT][DP + 1];  // this item's rows (odd stride)
-    float cols[kCT][DP + 1];  // one column tile
+    uint64_t rows2[kRT][DP];         // this item's rows, each coordinate duplicated into both halves
+    uint64_t cols2[kCT / 2][DP + 1];  // one column tile as packed column pairs (odd stride)
     int item;
 };
-
-// Exact squared distance chain of rows (r, r + 1) against one column (lane's),
-// both written into s0, s1 (the oracle's formula, bit for bit).
-template <int DP, bool PACKED>
-__device__ __forceinline__ void dist_pair(const BatchSmem<DP>& sh, int r, const float (&col)[DP], int d, float& s0,
-                                          float& s1) {
-    if constexpr (PACKED) {
-        uint64_t s2 = 0;
-#pragma unroll
-        for (int f = 0; f < DP; ++f) {
-            if (f < d) {
-                const uint64_t a2 = (static_cast<uint64_t>(__float_as_uint(sh.rows[r + 1][f])) << 32) |
-                                    __float_as_uint(sh.rows[r][f]);
-                uint64_t t2;
-                asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(t2) : "l"(a2), "l"(dup2(col[f])));
-                s2 = fma2(t2, t2, s2);
-            }
-        }
-        s0 = lo_f(s2);
-        s1 = hi_f(s2);
-    } else {
-        float a = 0.0f, b = 0.0f;
-#pragma unroll
-        for (int f = 0; f < DP; ++f) {
-            if (f < d) {
-                const float t0 = __fsub_rn(sh.rows[r][f], col[f]);
-                const float t1 = __fsub_rn(sh.rows[r + 1][f], col[f]);
-                a = __fmaf_rn(t0, t0, a);
-                b = __fmaf_rn(t1, t1, b);
-            }
-        }
-        s0 = a;
-        s1 = b;
-    }
-}
 
 // Append this lane's key for row r (if it beats the row's k-th key), keeping
 // 32 free slots: warp-uniform.
@@ -163,7 +128,24 @@ __device__ __forceinline__ void offer(RowLists<kBM>& L, int r, uint64_t key, int
     __syncwarp();
 }
 
-template <int DP, bool PACKED>
+// Offer a row's 2 * CP keys (one warp-uniform test first).
+template <int CP>
+__device__ __forceinline__ void offer_row(RowLists<kBM>& L, int r, const uint64_t (&key)[2 * CP], int k) {
+    uint64_t mn = key[0];
+#pragma unroll
+    for (int q = 1; q < 2 * CP; ++q) mn = key[q] < mn ? key[q] : mn;
+    if (!__any_sync(0xffffffffu, mn < L.kth[r])) return;
+#pragma unroll
+    for (int q = 0; q < 2 * CP; ++q) offer(L, r, key[q], k);
+}
+
+// Each warp owns 16 rows of the item. The CTA stages the problem's columns
+// in tiles of 128 (packed column pairs in shared memory); per pass a lane
+// holds CP column pairs in registers (packed f32x2 per dimension), so two
+// rows x CP pairs give 2 * CP independent packed FMA chains. Distances are
+// the oracle's direct-difference chain, exactly (per-lane IEEE sub.rn /
+// fma.rn).
+template <int DP, int CP>
 __global__ void __launch_bounds__(kThreads)
 batched_knn_kernel(const float* __restrict__ xc, const int64_t* __restrict__ off, const int* __restrict__ ks,
                    const int64_t* __restrict__ nkoff, const uint2* __restrict__ items, int nitems, int d,
@@ -172,6 +154,7 @@ batched_knn_kernel(const float* __restrict__ xc, const int64_t* __restrict__ off
     extern __shared__ __align__(16) unsigned char braw[];
     BatchSmem<DP>& sh = *reinterpret_cast<BatchSmem<DP>*>(braw);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    constexpr int kTile = 64 * CP;
     for (;;) {
         if (tid == 0) sh.item = static_cast<int>(atomicAdd(counter, 1u));
         __syncthreads();
@@ -186,7 +169,7 @@ batched_knn_kernel(const float* __restrict__ xc, const int64_t* __restrict__ off
         const int r0 = T * kRT;
         for (int i = tid; i < kRT * DP; i += kThreads) {
             const int r = i / DP, f = i % DP;
-            sh.rows[r][f] = (r0 + r < n && f < d) ? xp[static_cast<int64_t>(r0 + r) * d + f] : 0.0f;
+            sh.rows2[r][f] = dup2((r0 + r < n && f < d) ? xp[static_cast<int64_t>(r0 + r) * d + f] : 0.0f);
         }
         if (tid < kRT) {
             sh.L.cnt[tid] = 0;
@@ -194,36 +177,70 @@ batched_knn_kernel(const float* __restrict__ xc, const int64_t* __restrict__ off
             sh.L.row_norm[tid] = 0.0f;
         }
         __syncthreads();
+        const int rw = warp * kRowsPerWarp;
+#pragma unroll 1
         for (int c0 = 0; c0 < n; c0 += kCT) {
+            // the CTA stages 128 columns (coalesced) as packed pairs
             for (int i = tid; i < kCT * DP; i += kThreads) {
                 const int c = i / DP, f = i % DP;
-                sh.cols[c][f] = (c0 + c < n && f < d) ? xp[static_cast<int64_t>(c0 + c) * d + f] : 0.0f;
+                const float v = (c0 + c < n && f < d) ? xp[static_cast<int64_t>(c0 + c) * d + f] : 0.0f;
+                reinterpret_cast<float*>(&sh.cols2[c >> 1][f])[c & 1] = v;
             }
             __syncthreads();
 #pragma unroll 1
-            for (int sub = 0; sub < kCT / 32; ++sub) {
-                const int c = sub * 32 + lane;
-                const int gc = c0 + c;
-                float col[DP];
+            for (int sub = 0; sub < kCT; sub += kTile) {
+            uint64_t cp[CP][DP];
+            int cc[CP];
 #pragma unroll
-                for (int f = 0; f < DP; ++f) col[f] = sh.cols[c][f];
+            for (int q = 0; q < CP; ++q) {
+                const int pr = (sub >> 1) + 32 * q + lane;  // column pair index in the tile
+                cc[q] = c0 + 2 * pr;
+#pragma unroll
+                for (int f = 0; f < DP; ++f) cp[q][f] = sh.cols2[pr][f];
+            }
 #pragma unroll 1
-                for (int rr = 0; rr < kRowsPerWarp; rr += 2) {
-                    const int r = warp * kRowsPerWarp + rr;
-                    if (r0 + r >= n) break;  // warp-uniform: rows beyond the problem
-                    float s0, s1;
-                    dist_pair<DP, PACKED>(sh, r, col, d, s0, s1);
-                    const bool ok0 = gc < n && gc != r0 + r;
-                    const bool ok1 = gc < n && gc != r0 + r + 1 && r0 + r + 1 < n;
-                    offer(sh.L, r, ok0 ? make_key(__float_as_uint(s0), static_cast<uint32_t>(gc)) : kKeyMax, k);
-                    offer(sh.L, r + 1, ok1 ? make_key(__float_as_uint(s1), static_cast<uint32_t>(gc)) : kKeyMax, k);
+            for (int rr = 0; rr < kRowsPerWarp; rr += 2) {
+                const int r = rw + rr;
+                if (r0 + r >= n) break;  // warp-uniform: rows beyond the problem
+                uint64_t s[2][CP];
+#pragma unroll
+                for (int h = 0; h < 2; ++h)
+#pragma unroll
+                    for (int q = 0; q < CP; ++q) s[h][q] = 0;
+#pragma unroll
+                for (int f = 0; f < DP; ++f) {
+                    if (f < d) {
+                        const uint64_t a0 = sh.rows2[r][f], a1 = sh.rows2[r + 1][f];
+#pragma unroll
+                        for (int q = 0; q < CP; ++q) {
+                            uint64_t t0, t1;
+                            asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(t0) : "l"(a0), "l"(cp[q][f]));
+                            asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(t1) : "l"(a1), "l"(cp[q][f]));
+                            s[0][q] = fma2(t0, t0, s[0][q]);
+                            s[1][q] = fma2(t1, t1, s[1][q]);
+                        }
+                    }
                 }
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int gr = r0 + r + h;
+                    uint64_t key[2 * CP];
+#pragma unroll
+                    for (int q = 0; q < CP; ++q) {
+                        const int ca = cc[q], cb = cc[q] + 1;
+                        key[2 * q] = (gr < n && ca < n && ca != gr) ? make_key(__float_as_uint(lo_f(s[h][q])), ca) : kKeyMax;
+                        key[2 * q + 1] =
+                            (gr < n && cb < n && cb != gr) ? make_key(__float_as_uint(hi_f(s[h][q])), cb) : kKeyMax;
+                    }
+                    offer_row<CP>(sh.L, r + h, key, k);
+                }
+            }
             }
             __syncthreads();
         }
         // the k best per row, written in the reference's slot order
         for (int rr = 0; rr < kRowsPerWarp; ++rr) {
-            const int r = warp * kRowsPerWarp + rr;
+            const int r = rw + rr;
             const int il = r0 + r;
             if (il >= n) break;
             compact_row<kBM>(sh.L, r, k, 0.0f, 8);
@@ -305,35 +322,30 @@ __global__ void pid_kernel(const int64_t* __restrict__ off, int num, int* __rest
 
 int dp_for(int d) { return d <= 4 ? 4 : d <= 8 ? 8 : d <= 16 ? 16 : d <= 32 ? 32 : 64; }
 
-template <int DP, bool PACKED>
+template <int DP, int CP>
 void launch_knn_t(int grid, const BatchDev& b, cudaStream_t s) {
     const size_t smem = sizeof(BatchSmem<DP>);
     static bool configured = false;
     if (!configured) {
-        CG_CUDA(cudaFuncSetAttribute(batched_knn_kernel<DP, PACKED>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        CG_CUDA(cudaFuncSetAttribute(batched_knn_kernel<DP, CP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      static_cast<int>(smem)));
         configured = true;
     }
-    batched_knn_kernel<DP, PACKED><<<grid, kThreads, smem, s>>>(b.xc, b.off, b.ks, b.nkoff, b.items, b.nitems, b.d,
-                                                               b.counter, b.nbr, b.d2, b.kd);
+    batched_knn_kernel<DP, CP><<<grid, kThreads, smem, s>>>(b.xc, b.off, b.ks, b.nkoff, b.items, b.nitems, b.d,
+                                                           b.counter, b.nbr, b.d2, b.kd);
     CG_LAUNCH_CHECK();
 }
 
-void launch_knn(int dp, bool packed, int grid, const BatchDev& b, cudaStream_t s) {
-#define CG_B(DPV)                                                    \
-    case DPV:                                                        \
-        if (packed && DPV <= 32) launch_knn_t<DPV, true>(grid, b, s); \
-        else launch_knn_t<DPV, false>(grid, b, s);                   \
-        break;
+// cp2: two column pairs per lane (d <= 16), else one.
+void launch_knn(int dp, bool cp2, int grid, const BatchDev& b, cudaStream_t s) {
     switch (dp) {
-        CG_B(4)
-        CG_B(8)
-        CG_B(16)
-        CG_B(32)
-        CG_B(64)
+        case 4: cp2 ? launch_knn_t<4, 2>(grid, b, s) : launch_knn_t<4, 1>(grid, b, s); break;
+        case 8: cp2 ? launch_knn_t<8, 2>(grid, b, s) : launch_knn_t<8, 1>(grid, b, s); break;
+        case 16: cp2 ? launch_knn_t<16, 2>(grid, b, s) : launch_knn_t<16, 1>(grid, b, s); break;
+        case 32: launch_knn_t<32, 1>(grid, b, s); break;
+        case 64: launch_knn_t<64, 1>(grid, b, s); break;
         default: throw Error(kInternal, "bad padded dimension");
     }
-#undef CG_B
 }
 
 template <int DP>
@@ -483,7 +495,7 @@ void Engine::batch_autotune(const float* d_x, float* d_scores) {
     CG_CUDA(cudaEventCreate(&e1));
     float best = 1e30f;
     for (int per = 1; per <= max_per_sm; ++per) {
-        for (int packed = 0; packed <= (dp <= 32 ? 1 : 0); ++packed) {
+        for (int packed = 0; packed <= (dp <= 16 ? 1 : 0); ++packed) {
             btune_grid_ = per * sms;
             btune_packed_ = packed != 0;
             batch_launch(d_x, d_scores);  // warm (first use configures the kernel)
