@@ -73,6 +73,8 @@ def parse_args():
     p.add_argument("--cpu-seconds", type=float, default=8.0, help="target CPU time of the baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--path", choices=["auto", "fast", "general", "tensor"], default="auto")
+    p.add_argument("--suite", action="store_true",
+                   help="report harness: one JSON line per benchmark configuration (0-4) with an agreement gate")
     p.add_argument("--workload", choices=["clusters", "factor", "mixture"], default="clusters",
                    help="clusters: 5 clusters + 1%% outliers; factor: rank-16 factor model + 5.0 shift + 0.5%% noisy "
                         "rows; mixture: 8 clusters + 1%% outliers")
@@ -457,8 +459,152 @@ def run_ours(args):
     return 0
 
 
+# ----------------------------------------------------------------- report suite
+
+
+def _time_calls(fn, stream, warm=2, reps=5):
+    """Mean ms per call of fn (queued on stream), CUDA events around reps calls."""
+    import torch
+
+    for _ in range(warm):
+        fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def run_suite(args):
+    """One JSON line per benchmark configuration, each with its timing and an
+    agreement gate against the oracle or an independent exact path (the
+    speed and accuracy columns come from the same run)."""
+    import torch
+
+    import oracle
+    from culof_gb300 import _culof, synthetic
+    from oracle import backward as ob
+
+    torch.cuda.set_device(0)
+    stream = torch.cuda.current_stream()
+    dev = _culof.device_info()
+
+    def emit(line):
+        line["device"] = dev
+        print(json.dumps(line), flush=True)
+
+    def fit_predict_case(name, X, k, c, path, rows_checked):
+        n, d = X.shape
+        ctx = _culof.Context()
+        ctx.set_stream(stream.cuda_stream)
+        ctx.set_path(path)
+        dX = torch.from_numpy(X).cuda()
+        nof = torch.empty(n, device="cuda")
+        lab = torch.empty(n, dtype=torch.int64, device="cuda")
+        off = torch.empty(1, dtype=torch.float64, device="cuda")
+        ms = _time_calls(lambda: ctx.fit_predict_device(dX.data_ptr(), n, d, k, False, c, nof.data_ptr(),
+                                                        lab.data_ptr(), off.data_ptr()), stream)
+        # k-NN of a seeded block of rows against the oracle, bit for bit
+        idx = torch.empty((k, n), dtype=torch.int32, device="cuda")
+        d2 = torch.empty((k, n), device="cuda")
+        kd = torch.empty(n, device="cuda")
+        ctx.knn_device(dX.data_ptr(), n, d, k, False, idx.data_ptr(), d2.data_ptr(), kd.data_ptr())
+        ctx.synchronize()
+        b = int(np.random.default_rng(n).integers(0, n - rows_checked + 1))
+        Xc, _, _ = oracle.center(X)
+        t0 = time.perf_counter()
+        oi, od, ok = oracle.knn(Xc, k, rows=(b, b + rows_checked))
+        cpu_s = time.perf_counter() - t0
+        gi, gd, gk = idx.cpu().numpy(), d2.cpu().numpy(), kd.cpu().numpy()
+        agree = bool(np.array_equal(gi[:, b:b + rows_checked], oi[:, b:b + rows_checked])
+                     and np.array_equal(gd[:, b:b + rows_checked].view(np.uint32), od[:, b:b + rows_checked].view(np.uint32))
+                     and np.array_equal(gk[b:b + rows_checked].view(np.uint32), ok[b:b + rows_checked].view(np.uint32)))
+        res = {"suite": name, "n": n, "d": d, "k": k, "path": PATH_NAMES[ctx.last_path()],
+               "fit_predict_s": ms * 1e-3, "pair_dists_per_s": float(n) * n / (ms * 1e-3),
+               "agreement": {"knn_rows_checked": rows_checked, "bit_exact_vs_oracle": agree},
+               "cpu_oracle_knn_rows_per_s": rows_checked / cpu_s}
+        ctx.close()
+        return res, nof.cpu().numpy()
+
+    # config 0 and 1: clusters, d = 8, k = 20, c = 0.01
+    for name, n in (("config0", 20_000), ("config1", 200_000)):
+        X = synthetic.clusters_with_outliers(n, 8, seed=1)
+        res, _ = fit_predict_case(name, X, 20, 0.01, 0, 2000)
+        emit(res)
+    # config 2: factor model, d = 128, k = 50: tensor path against the FP32 sweep
+    X = synthetic.factor_model(200_000, 128, seed=1)
+    tres, tnof = fit_predict_case("config2", X, 50, 0.01, 3, 500)
+    fres, fnof = fit_predict_case("config2_fp32", X, 50, 0.01, 1, 1)
+    tres["fp32_fit_predict_s"] = fres["fit_predict_s"]
+    tres["speedup_vs_fp32"] = fres["fit_predict_s"] / tres["fit_predict_s"]
+    tres["agreement"]["nof_bit_exact_vs_fp32_path"] = bool(np.array_equal(tnof.view(np.uint32), fnof.view(np.uint32)))
+    emit(tres)
+    # config 3: sparse backward, n = 50,000, d = 32, k = 20
+    from culof_gb300.autograd import lof_scores
+
+    X = synthetic.gradient_mixture(50_000, 32, seed=1)
+    w = torch.from_numpy(np.random.default_rng(3).standard_normal(len(X))).cuda()
+    Xt = torch.from_numpy(X).cuda()
+
+    def fwd_bwd():
+        Xg = Xt.clone().requires_grad_(True)
+        (lof_scores(Xg, 20).double() * w).sum().backward()
+        return Xg.grad
+
+    ms_fb = _time_calls(fwd_bwd, stream)
+    ms_f = _time_calls(lambda: lof_scores(Xt, 20), stream)
+    g = fwd_bwd().double()
+    with _culof.Context() as ctx:
+        idx = torch.empty((20, len(X)), dtype=torch.int32, device="cuda")
+        d2 = torch.empty((20, len(X)), device="cuda")
+        kd = torch.empty(len(X), device="cuda")
+        ctx.knn_device(Xt.data_ptr(), len(X), 32, 20, False, idx.data_ptr(), d2.data_ptr(), kd.data_ptr())
+        ctx.synchronize()
+    X64 = Xt.double().requires_grad_(True)
+    (ob.lof_fixed(X64, idx.long(), False) * w).sum().backward()
+    rel = float((g - X64.grad).abs().max() / X64.grad.abs().max())
+    emit({"suite": "config3", "n": len(X), "d": 32, "k": 20, "forward_s": ms_f * 1e-3,
+          "backward_s": (ms_fb - ms_f) * 1e-3, "forward_backward_s": ms_fb * 1e-3,
+          "agreement": {"grad_max_rel_err_vs_fp64_autograd": rel, "float32_result": True}})
+    # config 4: 2,048 problems in one batched call against a loop of single calls
+    probs, ks = synthetic.batched_problems(2048, 16, seed=0)
+    Xb = np.concatenate(probs).astype(np.float32)
+    offs = np.zeros(len(probs) + 1, np.int64)
+    offs[1:] = np.cumsum([len(p) for p in probs])
+    ctx = _culof.Context()
+    ctx.set_stream(stream.cuda_stream)
+    dX = torch.from_numpy(Xb).cuda()
+    ds = torch.empty(len(Xb), device="cuda")
+    t0 = time.perf_counter()
+    ctx.lof_batched_device(offs, ks, dX.data_ptr(), 16, False, ds.data_ptr())
+    ctx.synchronize()
+    first_s = time.perf_counter() - t0
+    ms_b = _time_calls(lambda: ctx.lof_batched_device(offs, ks, dX.data_ptr(), 16, False, ds.data_ptr()), stream)
+    dps = [dX[offs[i]:offs[i + 1]] for i in range(len(probs))]
+    outs = torch.empty_like(ds)
+
+    def loop():
+        for i in range(len(probs)):
+            ctx.lof_device(dps[i].data_ptr(), len(probs[i]), 16, ks[i], False, outs[offs[i]:offs[i + 1]].data_ptr())
+
+    ms_l = _time_calls(loop, stream, warm=1, reps=2)
+    same = bool(np.array_equal(ds.cpu().numpy().view(np.uint32), outs.cpu().numpy().view(np.uint32)))
+    emit({"suite": "config4", "problems": len(probs), "points": int(offs[-1]), "d": 16,
+          "pairs": float(sum(float(len(p)) ** 2 for p in probs)),
+          "batched_s": ms_b * 1e-3, "loop_of_single_calls_s": ms_l * 1e-3, "speedup_vs_loop": ms_l / ms_b,
+          "first_call_s_plan_autotune_capture": first_s,
+          "agreement": {"bit_exact_vs_single_calls": same}})
+    ctx.close()
+    return 0
+
+
 def main():
     args = parse_args()
+    if args.suite:
+        return run_suite(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)
