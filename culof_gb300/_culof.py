@@ -78,6 +78,7 @@ _SIGS = {
     "culof_context_lof_backward_device": ([_P, _P, _I64, _I, _I, _I, _P, _P, _P, _P], _I),
     "culof_context_lof_batched_device": ([_P, _I, _P, _P, _P, _I, _I, _P], _I),
     "culof_context_set_graphs": ([_P, _I], _I),
+    "culof_context_pair_stats": ([_P, ctypes.POINTER(_D), ctypes.POINTER(_D)], _I),
     "culof_compute_scores": ([_P, _P, _P, _I64, _I, _P], _I),
     "culof_context_contamination_offset_device": ([_P, _P, _I64, _D, _P], _I),
     "culof_contamination_offset_noalloc": ([_P, _P, _I64, _D, _P], _I),
@@ -290,6 +291,12 @@ class Context:
             raise ValueError("offsets must have one more entry than ks")
         _check(_lib.culof_context_lof_batched_device(self._h, int(kk.shape[0]), off.ctypes.data, kk.ctypes.data,
                                                      points, int(d), int(bool(normalize)), scores))
+
+    def pair_stats(self):
+        """(evaluated pairs, unpruned pairs) of the last small-d FP32 sweep."""
+        ev, tot = _D(0.0), _D(0.0)
+        _check(_lib.culof_context_pair_stats(self._h, ctypes.byref(ev), ctypes.byref(tot)))
+        return ev.value, tot.value
 
     def set_graphs(self, on: bool) -> None:
         _check(_lib.culof_context_set_graphs(self._h, int(bool(on))))

@@ -151,6 +151,10 @@ int culof_context_stage_times(culof_context* ctx, float* ms, int cap) {
 
 unsigned long long culof_kernel_launch_count(void) { return culof_gb300::launch_count(); }
 
+int culof_context_pair_stats(culof_context* ctx, double* evaluated_pairs, double* total_pairs) {
+    return guarded([&] { engine_of(ctx).pair_stats(evaluated_pairs, total_pairs); });
+}
+
 int culof_lof(const float* points, int64_t n_points, int n_dims, int k, int normalize, float* scores_out) {
     return guarded([&] {
         culof_gb300::validate_lof_args(points, n_points, n_dims, k);

@@ -144,6 +144,7 @@ void Engine::knn(const float* d_x, int64_t n, int d, int k, bool normalize, int3
     float* norms = norms_.as<float>(n);
     unsigned int* maxn = max_norm_.as<unsigned int>(1);
     CG_CUDA(cudaMemsetAsync(status_ptr(), 0, sizeof(int), stream_));
+    stat_total_blocks_ = 0;
     for (bool& m : marked_) m = false;
     mark(0);
     center(d_x, n, d, normalize, xc, partial, mean, inv, stream_);
@@ -235,6 +236,18 @@ void Engine::stage_times(float* ms, int cap) {
         ms[i] = -1.0f;
         if (timing_ && marked_[i] && marked_[i + 1]) CG_CUDA(cudaEventElapsedTime(&ms[i], events_[i], events_[i + 1]));
     }
+}
+
+void Engine::pair_stats(double* evaluated, double* total) {
+    unsigned long long ev = 0;
+    if (stat_total_blocks_ > 0) {
+        CG_CUDA(cudaMemcpyAsync(&ev, pair_stats_.get(2 * sizeof(unsigned long long)), sizeof(ev),
+                                cudaMemcpyDeviceToHost, stream_));
+        CG_CUDA(cudaStreamSynchronize(stream_));
+    }
+    // one block = 16 rows x 128 columns
+    if (evaluated) *evaluated = static_cast<double>(ev) * 16.0 * 128.0;
+    if (total) *total = static_cast<double>(stat_total_blocks_) * 16.0 * 128.0;
 }
 
 void Engine::check_status() {

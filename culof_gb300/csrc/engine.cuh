@@ -91,6 +91,9 @@ public:
     void lof_batched_device(int num, const int64_t* offsets, const int* ks, const float* d_x, int d, bool normalize,
                             float* d_scores);
     void set_graphs(bool on) { use_graphs_ = on; }
+    // Pairs the last FP32 small-d sweep evaluated and the pairs of an
+    // unpruned sweep (both 0 for other paths); synchronises.
+    void pair_stats(double* evaluated, double* total);
     void lof_backward_device(const float* d_x, int64_t n, int d, int k, bool normalize, const int32_t* nbr_idx,
                              const double* grad_scores, double* grad_x, double* scores_out);
 
@@ -136,6 +139,10 @@ private:
     unsigned long long bgraph_kernels_ = 0;
     // fast path workspaces
     DevBuf morton_, perm_, sort_tmp_, sort_hist_, cols_, rows_, tc_lists_;
+    // the FP32 sweep's evaluated (warp x column tile) blocks; the total it
+    // would evaluate without pruning
+    DevBuf pair_stats_, boxes_, plist_, pcount_;
+    unsigned long long stat_total_blocks_ = 0;
     // Device status word of the current call: kernels set it (a bounded wait
     // that expired, an out-of-range neighbour index); host paths check it.
     DevBuf status_;

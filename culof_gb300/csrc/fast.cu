@@ -31,6 +31,7 @@
 // decides which pairs get an exact evaluation, and its bound is proven
 // conservative (tau_from below).
 #include <cmath>
+#include <cstdlib>
 
 #include "common.cuh"
 #include "engine.cuh"
@@ -60,11 +61,14 @@ constexpr int kMortonDims = 8;  // Morton key over (up to) the 8 widest dimensio
 //           that eight pair records read by one warp hit distinct banks
 //   norms : kCT floats (NaN for padding columns)
 //   index : kCT uint32 original indices (kNoIndex for padding)
+//   box   : per-dimension minimum and maximum over the tile's valid points
 // The CTA's own rows are the columns of its own tile.
 __host__ __device__ constexpr int pair_stride(int dp) { return ((2 * dp / 4) % 2 == 1) ? 2 * dp : 2 * dp + 4; }
 __host__ __device__ constexpr int tile_norms_off(int dp) { return kPairs * pair_stride(dp); }
 __host__ __device__ constexpr int tile_index_off(int dp) { return tile_norms_off(dp) + kCT; }
-__host__ __device__ constexpr int tile_floats(int dp) { return tile_index_off(dp) + kCT; }
+// bounding box of the tile's valid points: lo[DP], hi[DP] (padding dims 0)
+__host__ __device__ constexpr int tile_box_off(int dp) { return tile_index_off(dp) + kCT; }
+__host__ __device__ constexpr int tile_floats(int dp) { return tile_box_off(dp) + 2 * dp; }
 __host__ __device__ constexpr int tile_bytes(int dp) { return tile_floats(dp) * 4; }
 
 // Coordinate f of column c within a tile.
@@ -314,6 +318,127 @@ __device__ __forceinline__ float tile_dist2(const float* ta, int ca, const float
 // Per row of tile T: the exact k best keys over tile T's own columns (sorted,
 // kKeyMax padded) and its k-th key, the starting point of the row's shared
 // k-th key (kth_shared) that the sweep CTAs tighten with atomicMin.
+// Pruning margin: the float32 direct-difference distance D of two points at
+// real squared distance T >= LB satisfies D >= T (1 - (d + 2) 2^-24) >
+// LB (1 - 2^-20) for d <= 8, so a tile whose rounded-down box gap times
+// (1 - 2^-20) exceeds every row's k-th distance holds no candidate.
+constexpr float kPruneShrink = 0.99999904632568359375f;  // 1 - 2^-20
+
+// One warp per tile: the bounding box of its valid points (the sweep's
+// pruning test reads it with the tile).
+template <int DP>
+__global__ void tile_box_kernel(float* __restrict__ tiles, int nt, float* __restrict__ boxes) {
+    const int lane = threadIdx.x & 31;
+    const int t = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (t >= nt) return;
+    float* tile = tiles + static_cast<int64_t>(t) * tile_floats(DP);
+    const unsigned* idx = reinterpret_cast<const unsigned*>(tile + tile_index_off(DP));
+#pragma unroll
+    for (int f = 0; f < DP; ++f) {
+        float lo = __int_as_float(0x7f800000), hi = __int_as_float(0xff800000);
+        for (int c = lane; c < kCT; c += 32) {
+            if (idx[c] != kNoIndex) {
+                const float v = tile_coord<DP>(tile, c, f);
+                lo = fminf(lo, v);
+                hi = fmaxf(hi, v);
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+            hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+        }
+        if (lane == 0) {
+            tile[tile_box_off(DP) + f] = lo;
+            tile[tile_box_off(DP) + DP + f] = hi;
+            boxes[static_cast<int64_t>(t) * 2 * DP + f] = lo;
+            boxes[static_cast<int64_t>(t) * 2 * DP + DP + f] = hi;
+        }
+    }
+}
+
+// Squared distance between two boxes, rounded down (a lower bound of the
+// real squared distance of any two points in them): lane f < DP takes
+// dimension f, the sum runs with round-down additions. Warp-uniform result.
+template <int DP>
+__device__ __forceinline__ float box_gap2_rd(const float* __restrict__ a_lo, const float* __restrict__ a_hi,
+                                             const float* __restrict__ b_lo, const float* __restrict__ b_hi) {
+    const int lane = threadIdx.x & 31;
+    float g = 0.0f;
+    if (lane < DP) {
+        const float g1 = __fsub_rd(b_lo[lane], a_hi[lane]);
+        const float g2 = __fsub_rd(a_lo[lane], b_hi[lane]);
+        const float gap = fmaxf(0.0f, fmaxf(g1, g2));
+        g = __fmul_rd(gap, gap);
+    }
+#pragma unroll
+    for (int o = 4; o > 0; o >>= 1) g = __fadd_rd(g, __shfl_xor_sync(0xffffffffu, g, o));
+    return __shfl_sync(0xffffffffu, g, 0);
+}
+
+// Per row tile T (one block): the column tiles that can hold a candidate for
+// any of its rows under the seed's k-th distances, in the sweep's visiting
+// order, each with its rounded-down box gap (the sweep re-tests the gap
+// against its tighter current k-th distances without touching the boxes).
+template <int DP>
+__global__ void __launch_bounds__(256) prune_list_kernel(const float* __restrict__ boxes, int nt,
+                                                         const unsigned long long* __restrict__ kth_seed,
+                                                         uint2* __restrict__ plist, int* __restrict__ pcount) {
+    __shared__ float tbox[2][DP];
+    __shared__ float kmax_s;
+    __shared__ int wtot[8];
+    __shared__ int base_s;
+    const int T = blockIdx.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x < 2 * DP) tbox[threadIdx.x / DP][threadIdx.x % DP] = boxes[static_cast<int64_t>(T) * 2 * DP + threadIdx.x];
+    if (warp == 0) {
+        float v = __int_as_float(0xff800000);
+        for (int r = lane; r < kRT; r += 32) {
+            const unsigned long long kk = kth_seed[static_cast<int64_t>(T) * kRT + r];
+            v = fmaxf(v, kk == kKeyMax ? __int_as_float(0x7f800000) : __uint_as_float(key_bits(kk)));
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+        if (lane == 0) {
+            kmax_s = v;
+            base_s = 0;
+        }
+    }
+    __syncthreads();
+    const float kmax = kmax_s;
+    uint2* out = plist + static_cast<int64_t>(T) * nt;
+    for (int q0 = 1; q0 < nt; q0 += 256) {
+        const int q = q0 + static_cast<int>(threadIdx.x);
+        bool pass = false;
+        unsigned t = 0;
+        float g2 = 0.0f;
+        if (q < nt) {
+            t = static_cast<unsigned>(spiral_tile(T, q, nt));
+            const float* b = boxes + static_cast<int64_t>(t) * 2 * DP;
+#pragma unroll
+            for (int f = 0; f < DP; ++f) {
+                const float gap = fmaxf(0.0f, fmaxf(__fsub_rd(b[f], tbox[1][f]), __fsub_rd(tbox[0][f], b[DP + f])));
+                g2 = __fadd_rd(g2, __fmul_rd(gap, gap));
+            }
+            pass = !(__fmul_rd(g2, kPruneShrink) > kmax);
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, pass);
+        if (lane == 0) wtot[warp] = __popc(m);
+        __syncthreads();
+        int before = base_s;
+        for (int w = 0; w < warp; ++w) before += wtot[w];
+        if (pass) out[before + __popc(m & ((1u << lane) - 1u))] = make_uint2(t, __float_as_uint(g2));
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int tot = 0;
+            for (int w = 0; w < 8; ++w) tot += wtot[w];
+            base_s += tot;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) pcount[T] = base_s;
+}
+
 template <int DP>
 __global__ void __launch_bounds__(kThreads) seed_kernel(const float* __restrict__ tiles, int nt, int64_t n, int k,
                                                         uint64_t* __restrict__ seed_keys,
@@ -365,7 +490,15 @@ struct SweepSmem {
     uint64_t rowd[kRT][DP];  // (-2a, -2a) per row and dimension: the packed FMA operands
     int done[kStages];
     uint16_t queue[kWarps][kQueueCap];
+    float wbox[kWarps][2][DP];  // bounding box of each warp's 16 rows
+    float wkmax[kWarps];        // largest k-th distance among each warp's rows
+    float cbox[2][DP];          // bounding box of the CTA's rows
+    int stage_tile[kStages];    // column tile in each stage, -1: the split is done
+    int last_fill[kStages];     // fill number of the stage's last tile copy (-1: none)
+    int next_j;                 // the loader's scan position in the split's sequence
+    unsigned evaluated;         // warp x column-tile blocks evaluated (not pruned)
 };
+
 
 // Exact rescoring of the warp's queued candidates (one per lane): exact
 // distance, append to the row list if the key beats the row's k-th key;
@@ -406,7 +539,9 @@ __device__ bool drain_queue(SweepSmem<DP, M>& sh, int qc, const float* __restric
 template <int DP, int M>
 __global__ void __launch_bounds__(kThreads, 2)
 sweep_kernel(const float* __restrict__ tiles, int nt, int nsplit, int k, const unsigned* __restrict__ max_norm_bits,
-             unsigned long long* __restrict__ kth_shared, uint64_t* __restrict__ partial, int* __restrict__ status) {
+             unsigned long long* __restrict__ kth_shared, uint64_t* __restrict__ partial, int* __restrict__ status,
+             unsigned long long* __restrict__ evaluated_blocks, const uint2* __restrict__ plist,
+             const int* __restrict__ pcount) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     SweepSmem<DP, M>& sh = *reinterpret_cast<SweepSmem<DP, M>*>(smem_raw);
     const int T = blockIdx.x % nt;
@@ -414,11 +549,13 @@ sweep_kernel(const float* __restrict__ tiles, int nt, int nsplit, int k, const u
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const float nmax = __uint_as_float(*max_norm_bits);
     const float* own = tiles + static_cast<int64_t>(T) * tile_floats(DP);
-    // this split's contiguous run of visiting positions q in [q0, q1), q >= 1
-    const int per = (nt - 1 + nsplit - 1) / nsplit;
-    const int q0 = 1 + split * per;
-    const int q1 = min(nt, q0 + per);
-    const int count = q1 > q0 ? q1 - q0 : 0;
+    // this split's share of the row tile's candidate column tiles: entries
+    // split + nsplit j of its list (visiting order, interleaved, so every
+    // split meets the nearby tiles first)
+    // (without lists, very large n: every other tile in spiral order)
+    const int lcount = plist ? pcount[T] : nt - 1;
+    const int count = lcount > split ? (lcount - split + nsplit - 1) / nsplit : 0;
+    const uint2* tlist = plist ? plist + static_cast<int64_t>(T) * nt : nullptr;
     constexpr unsigned kTileBytes = tile_bytes(DP);
 
     if (tid < kRT) {
@@ -437,19 +574,17 @@ sweep_kernel(const float* __restrict__ tiles, int nt, int nsplit, int k, const u
             sh.rowd[tid][f] = dup2(-2.0f * sh.rowc[tid][f]);
         }
     }
-    if (tid < kStages) sh.done[tid] = 0;
+    if (tid < kStages) {
+        sh.done[tid] = 0;
+        sh.last_fill[tid] = -1;
+    }
     if (tid == 0) {
+        sh.evaluated = 0;
+        sh.next_j = 0;
         for (int s = 0; s < kStages; ++s) mbar_init(&sh.full_bar[s], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
-    if (tid == 0) {
-        for (int m = 0; m < kStages && m < count; ++m) {
-            const int t = spiral_tile(T, q0 + m, nt);
-            mbar_expect_tx(&sh.full_bar[m], kTileBytes);
-            tma_load_1d(sh.tiles[m], tiles + static_cast<int64_t>(t) * tile_floats(DP), kTileBytes, &sh.full_bar[m]);
-        }
-    }
     // lane = (row group g, pair slot cp): rows warp*16 + g*4 + j, pairs s*8 + cp
     const int g = lane >> 3, cp = lane & 7;
     const int rbase = warp * kRowsPerWarp + g * kRowsPerLane;
@@ -468,19 +603,117 @@ sweep_kernel(const float* __restrict__ tiles, int nt, int nsplit, int k, const u
         tau_r[j] = sh.L.tau[rbase + j];
         tau2[j] = dup2(tau_above(tau_r[j]));
     }
+    // this warp's row box and the largest k-th distance among its rows
+    // (invalid rows take no candidates and do not count)
+    const unsigned* own_idx = reinterpret_cast<const unsigned*>(own) + tile_index_off(DP);
+    const int wrow = warp * kRowsPerWarp + (lane & 15);
+    const bool wvalid = own_idx[wrow] != kNoIndex;
+#pragma unroll
+    for (int f = 0; f < DP; ++f) {
+        float lo = wvalid ? sh.rowc[wrow][f] : __int_as_float(0x7f800000);
+        float hi = wvalid ? sh.rowc[wrow][f] : __int_as_float(0xff800000);
+#pragma unroll
+        for (int o = 8; o > 0; o >>= 1) {
+            lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+            hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+        }
+        if (lane == 0) {
+            sh.wbox[warp][0][f] = lo;
+            sh.wbox[warp][1][f] = hi;
+        }
+    }
+    auto warp_kth = [&]() -> float {
+        const uint64_t kk = sh.L.kth[wrow];
+        float v = !wvalid ? __int_as_float(0xff800000)
+                          : (kk == kKeyMax ? __int_as_float(0x7f800000) : __uint_as_float(key_bits(kk)));
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+        return v;
+    };
+    __syncwarp();
+    float wk = warp_kth();
+    if (lane == 0) sh.wkmax[warp] = wk;
+
+    // The stage loader (one warp at a time): the next column tile of the
+    // split that can hold a candidate for some row of this CTA, tested 32 at
+    // a time against the CTA's row box and largest k-th distance (stale
+    // values only prune less); a stage with no tile left gets a sentinel.
+    auto fill = [&](int stage, int fill_no) {
+        float kmax = lane < kWarps ? sh.wkmax[lane] : __int_as_float(0xff800000);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) kmax = fmaxf(kmax, __shfl_xor_sync(0xffffffffu, kmax, o));
+        int found = -1;
+        int base = sh.next_j;
+        while (found < 0 && base < count) {
+            const int j = base + lane;
+            int t = -1;
+            bool pass = false;
+            if (j < count) {
+                if (tlist) {
+                    const uint2 e = __ldg(tlist + split + nsplit * j);
+                    t = static_cast<int>(e.x);
+                    pass = !(__fmul_rd(__uint_as_float(e.y), kPruneShrink) > kmax);
+                } else {
+                    t = spiral_tile(T, 1 + split + nsplit * j, nt);
+                    pass = true;
+                }
+            }
+            const unsigned mk = __ballot_sync(0xffffffffu, pass);
+            if (mk) {
+                const int o = __ffs(mk) - 1;
+                found = __shfl_sync(0xffffffffu, t, o);
+                base += o + 1;
+            } else {
+                base += 32;
+            }
+        }
+        if (lane == 0) {
+            sh.next_j = base;
+            if (found >= 0) {
+                sh.stage_tile[stage] = found;
+                sh.last_fill[stage] = fill_no;
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                mbar_expect_tx(&sh.full_bar[stage], kTileBytes);
+                tma_load_1d(sh.tiles[stage], tiles + static_cast<int64_t>(found) * tile_floats(DP), kTileBytes,
+                            &sh.full_bar[stage]);
+            } else {
+                sh.stage_tile[stage] = -1;
+                mbar_arrive_plain(&sh.full_bar[stage]);
+            }
+        }
+        __syncwarp();
+    };
+    __syncthreads();
+    if (tid < DP) {
+        float lo = __int_as_float(0x7f800000), hi = __int_as_float(0xff800000);
+        for (int w = 0; w < kWarps; ++w) {
+            lo = fminf(lo, sh.wbox[w][0][tid]);
+            hi = fmaxf(hi, sh.wbox[w][1][tid]);
+        }
+        sh.cbox[0][tid] = lo;
+        sh.cbox[1][tid] = hi;
+    }
+    __syncthreads();
+    if (warp == 0)
+        for (int st = 0; st < kStages; ++st) fill(st, st);
 
     bool ok = true;
-    for (int m = 0; m < count && ok; ++m) {
+    for (int m = 0; ok; ++m) {
         const int stage = m % kStages;
         if (!mbar_wait_warp(&sh.full_bar[stage], (m / kStages) & 1)) {
             ok = false;
             break;
         }
+        if (sh.stage_tile[stage] < 0) break;  // the split is done
         const float* tl = sh.tiles[stage];
         const float* tn = tl + tile_norms_off(DP);
         int qc = 0;
+        // prune: the whole tile is farther than every row's k-th distance
+        const float* tb = tl + tile_box_off(DP);
+        const bool skip = __fmul_rd(box_gap2_rd<DP>(sh.wbox[warp][0], sh.wbox[warp][1], tb, tb + DP), kPruneShrink) > wk;
+        if (!skip && lane == 0) atomicAdd(&sh.evaluated, 1u);
 #pragma unroll 2
-        for (int s = 0; s < kPairs / 8; ++s) {
+        for (int s = 0; s < (skip ? 0 : kPairs / 8); ++s) {
             const int p = s * 8 + cp;
             uint64_t B[DP];
 #pragma unroll
@@ -539,6 +772,8 @@ sweep_kernel(const float* __restrict__ tiles, int nt, int nsplit, int k, const u
                             tau_r[j] = sh.L.tau[rbase + j];
                             tau2[j] = dup2(tau_above(tau_r[j]));
                         }
+                        wk = warp_kth();
+                        if (lane == 0) sh.wkmax[warp] = wk;
                     }
                     qc = 0;
                 }
@@ -551,33 +786,29 @@ sweep_kernel(const float* __restrict__ tiles, int nt, int nsplit, int k, const u
                     tau_r[j] = sh.L.tau[rbase + j];
                     tau2[j] = dup2(tau_above(tau_r[j]));
                 }
+                wk = warp_kth();
+                if (lane == 0) sh.wkmax[warp] = wk;
             }
         }
-        // done with this stage; the last warp out refills it with tile m + kStages
+        // done with this stage; the last warp out refills it
         __syncwarp();
+        int prev = 0;
         if (lane == 0) {
             __threadfence_block();
-            const int prev = atomicAdd(&sh.done[stage], 1);
-            if (prev == kWarps - 1) {
-                sh.done[stage] = 0;
-                if (m + kStages < count) {
-                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                    const int t = spiral_tile(T, q0 + m + kStages, nt);
-                    mbar_expect_tx(&sh.full_bar[stage], kTileBytes);
-                    tma_load_1d(sh.tiles[stage], tiles + static_cast<int64_t>(t) * tile_floats(DP), kTileBytes,
-                                &sh.full_bar[stage]);
-                }
-            }
+            prev = atomicAdd(&sh.done[stage], 1);
+        }
+        prev = __shfl_sync(0xffffffffu, prev, 0);
+        if (prev == kWarps - 1) {
+            if (lane == 0) sh.done[stage] = 0;
+            fill(stage, m + kStages);
         }
     }
     const int failed = __syncthreads_or(ok ? 0 : 1);
+    if (tid == 0 && evaluated_blocks) atomicAdd(evaluated_blocks, static_cast<unsigned long long>(sh.evaluated));
     if (failed) {
         if (tid == 0) atomicExch(status, 1);
         // wait (bounded) for this CTA's copies still in flight before exiting
-        if (tid < kStages) {
-            for (int m = count - 1; m >= 0 && m >= count - kStages; --m)
-                if (m % kStages == tid) mbar_wait(&sh.full_bar[tid], (m / kStages) & 1);
-        }
+        if (tid < kStages && sh.last_fill[tid] >= 0) mbar_wait(&sh.full_bar[tid], (sh.last_fill[tid] / kStages) & 1);
         __syncthreads();
         return;
     }
@@ -684,7 +915,8 @@ namespace {
 
 template <int DP, int M>
 void launch_sweep(const float* tiles, int nt, int nsplit, int k, const unsigned* maxn, unsigned long long* kth_shared,
-                  uint64_t* partial, int* status, cudaStream_t s) {
+                  uint64_t* partial, int* status, unsigned long long* evaluated, const uint2* plist, const int* pcount,
+                  cudaStream_t s) {
     const size_t smem = sizeof(SweepSmem<DP, M>);
     static bool configured = false;  // per instantiation; the attribute is set once per process
     if (!configured) {
@@ -692,7 +924,8 @@ void launch_sweep(const float* tiles, int nt, int nsplit, int k, const unsigned*
                                      static_cast<int>(smem)));
         configured = true;
     }
-    sweep_kernel<DP, M><<<nt * nsplit, kThreads, smem, s>>>(tiles, nt, nsplit, k, maxn, kth_shared, partial, status);
+    sweep_kernel<DP, M><<<nt * nsplit, kThreads, smem, s>>>(tiles, nt, nsplit, k, maxn, kth_shared, partial, status,
+                                                            evaluated, plist, pcount);
     CG_LAUNCH_CHECK();
 }
 
@@ -754,7 +987,11 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
     CG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_));
     // The tensor sweep runs two CTAs per SM; with two or more waves of row
     // tiles a single column split keeps each row's final rescoring to one pass.
-    const int nsplit = nt <= 1 ? 1 : (tensor && nt >= 4 * sms) ? 1 : choose_splits(nt, sms);
+    int nsplit = nt <= 1 ? 1 : (tensor && nt >= 4 * sms) ? 1 : choose_splits(nt, sms);
+    if (const char* env = std::getenv("CULOF_SPLITS")) {  // tuning override (1..nt-1)
+        const long v = std::atol(env);
+        if (v >= 1 && nt > 1) nsplit = static_cast<int>(v < nt - 1 ? v : nt - 1);
+    }
 
     // 1. Morton keys of the centred coordinates, then a stable radix sort.
     unsigned* mm = reinterpret_cast<unsigned*>(sort_hist_.get(2 * sizeof(unsigned) * d + sizeof(int) * kMortonDims));
@@ -792,6 +1029,7 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
     // 2. column tiles
     float* tiles = nullptr;
     TcBuffers tcb{};
+    float* boxes = nullptr;
     if (tensor) {
         tcb = tc_prepare(cols_.get(tc_buffer_bytes(padded, d)), xc, norms, n, d, perm, nt, mm, s);
     } else if (wide) {
@@ -809,7 +1047,18 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
         case 6: build_tiles_kernel<6><<<grid_for(padded, 256), 256, 0, s>>>(xc, norms, n, d, perm, padded, tiles); break;
         default: build_tiles_kernel<8><<<grid_for(padded, 256), 256, 0, s>>>(xc, norms, n, d, perm, padded, tiles); break;
     }
-    if (!wide && !tensor) CG_LAUNCH_CHECK();
+    if (!wide && !tensor) {
+        CG_LAUNCH_CHECK();
+        boxes = boxes_.as<float>(static_cast<size_t>(nt) * 2 * dp);
+        const unsigned bg = static_cast<unsigned>(ceil_div(nt, 8));
+        switch (dp) {
+            case 2: tile_box_kernel<2><<<bg, 256, 0, s>>>(tiles, nt, boxes); break;
+            case 4: tile_box_kernel<4><<<bg, 256, 0, s>>>(tiles, nt, boxes); break;
+            case 6: tile_box_kernel<6><<<bg, 256, 0, s>>>(tiles, nt, boxes); break;
+            default: tile_box_kernel<8><<<bg, 256, 0, s>>>(tiles, nt, boxes); break;
+        }
+        CG_LAUNCH_CHECK();
+    }
 
     // 3. seed lists and the shared k-th keys
     char* rows = static_cast<char*>(rows_.get(padded * sizeof(uint64_t) * (k + 1) +
@@ -831,7 +1080,26 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
     if (!wide && !tensor) CG_LAUNCH_CHECK();
     mark(3);
 
+    // 3b. per row tile: the column tiles the seed's k-th distances leave
+    uint2* plist = nullptr;
+    int* pcount = nullptr;
+    constexpr int kMaxListTiles = 16384;  // lists take nt^2 x 8 bytes: up to 2 GiB
+    if (!wide && !tensor && nt > 1 && nt <= kMaxListTiles) {
+        plist = plist_.as<uint2>(static_cast<size_t>(nt) * nt);
+        pcount = pcount_.as<int>(nt);
+        switch (dp) {
+            case 2: prune_list_kernel<2><<<nt, 256, 0, s>>>(boxes, nt, kth_shared, plist, pcount); break;
+            case 4: prune_list_kernel<4><<<nt, 256, 0, s>>>(boxes, nt, kth_shared, plist, pcount); break;
+            case 6: prune_list_kernel<6><<<nt, 256, 0, s>>>(boxes, nt, kth_shared, plist, pcount); break;
+            default: prune_list_kernel<8><<<nt, 256, 0, s>>>(boxes, nt, kth_shared, plist, pcount); break;
+        }
+        CG_LAUNCH_CHECK();
+    }
+
     // 4. sweep over the other tiles, split S ways
+    unsigned long long* evaluated = reinterpret_cast<unsigned long long*>(pair_stats_.get(2 * sizeof(unsigned long long)));
+    CG_CUDA(cudaMemsetAsync(evaluated, 0, 2 * sizeof(unsigned long long), s));
+    stat_total_blocks_ = (!wide && !tensor && nt > 1) ? static_cast<unsigned long long>(nt) * (nt - 1) * kWarps : 0;
     if (nt > 1 && tensor) {
         uint64_t* lists = static_cast<uint64_t*>(tc_lists_.get(tc_list_bytes(nt, nsplit)));
         tc_sweep(tcb, nt, nsplit, d, k, maxn, kth_shared, partial, lists, status, s);
@@ -840,8 +1108,8 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
     } else if (nt > 1) {
         const bool big = k > 32;
 #define CG_SWEEP(DPV)                                                                                 \
-    (big ? launch_sweep<DPV, 96>(tiles, nt, nsplit, k, maxn, kth_shared, partial, status, s)          \
-         : launch_sweep<DPV, 64>(tiles, nt, nsplit, k, maxn, kth_shared, partial, status, s))
+    (big ? launch_sweep<DPV, 96>(tiles, nt, nsplit, k, maxn, kth_shared, partial, status, evaluated, plist, pcount, s) \
+         : launch_sweep<DPV, 64>(tiles, nt, nsplit, k, maxn, kth_shared, partial, status, evaluated, plist, pcount, s))
         switch (dp) {
             case 2: CG_SWEEP(2); break;
             case 4: CG_SWEEP(4); break;

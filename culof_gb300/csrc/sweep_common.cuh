@@ -101,6 +101,10 @@ __device__ __forceinline__ bool mbar_wait_warp(uint64_t* bar, unsigned parity) {
     }
     return false;
 }
+// Plain arrive (no transaction bytes): completes a phase that expects no copy.
+__device__ __forceinline__ void mbar_arrive_plain(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
 __device__ __forceinline__ void tma_load_1d(void* smem_dst, const void* gmem_src, unsigned bytes, uint64_t* bar) {
     asm volatile(
         "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
