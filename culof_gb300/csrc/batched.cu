@@ -8,12 +8,15 @@
 // problems (points concatenated, per-problem offsets and k):
 //   1. batched centring: the single-problem centring's arithmetic, in the
 //      same order (chunks of kCenterChunk rows), for every problem at once;
-//   2. a persistent k-NN kernel: CTAs pull (problem, 128-row tile) work items
-//      from an atomic counter, largest problems first, and select each row's
+//   2. a spatial order within each problem (Morton keys over its 8 widest
+//      dimensions, two stable radix sorts);
+//   3. a persistent k-NN kernel: CTAs pull (problem, 128-row tile) work items
+//      from an atomic counter, largest problems first, visit the problem's
+//      column tiles nearest first (spiral from the own tile) and select each row's
 //      exact k nearest among its problem's points (FP32 direct differences,
 //      the oracle's formula, two columns per packed f32x2 instruction) into
 //      per-row lists in shared memory;
-//   3. batched lrd and scores with the reference's FP64 sums.
+//   4. batched lrd and scores with the reference's FP64 sums.
 // Every problem's scores are bit-identical to a single-problem call. The
 // launch sequence of a given batch layout is captured once as a CUDA graph
 // and replayed; on first sight of a layout a small autotuner times the k-NN
@@ -26,6 +29,7 @@
 
 #include "common.cuh"
 #include "engine.cuh"
+#include "fast.cuh"
 #include "sweep_common.cuh"
 
 namespace culof_gb300 {
@@ -98,6 +102,162 @@ __global__ void bc_apply_kernel(const float* __restrict__ x, int64_t ntot, int d
     }
 }
 
+// ---- spatial order within each problem -----------------------------------------
+
+__device__ __forceinline__ unsigned flip_f(float f) {
+    const unsigned u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float unflip_f(unsigned k) {
+    return __uint_as_float((k & 0x80000000u) ? (k & 0x7FFFFFFFu) : ~k);
+}
+
+constexpr int kMortonDimsB = 8;
+
+// One block per problem: per-dimension range of its centred points, then
+// the (up to) 8 widest dimensions, widest first (ties by index).
+__global__ void bm_minmax_kernel(const float* __restrict__ xc, const int64_t* __restrict__ off, int d,
+                                 float* __restrict__ pmm, int* __restrict__ pdims) {
+    __shared__ unsigned lo[kBMaxD], hi[kBMaxD];
+    const int p = blockIdx.x;
+    for (int f = threadIdx.x; f < d; f += blockDim.x) {
+        lo[f] = 0xFFFFFFFFu;
+        hi[f] = 0u;
+    }
+    __syncthreads();
+    const int64_t b = off[p], e = off[p + 1];
+    for (int64_t t = threadIdx.x; t < (e - b) * d; t += blockDim.x) {
+        const int f = static_cast<int>(t % d);
+        const unsigned k = flip_f(xc[b * d + t]);
+        atomicMin(&lo[f], k);
+        atomicMax(&hi[f], k);
+    }
+    __syncthreads();
+    for (int f = threadIdx.x; f < d; f += blockDim.x) {
+        pmm[(static_cast<int64_t>(p) * d + f) * 2] = unflip_f(lo[f]);
+        pmm[(static_cast<int64_t>(p) * d + f) * 2 + 1] = unflip_f(hi[f]);
+    }
+    if (threadIdx.x == 0) {
+        const int m = d < kMortonDimsB ? d : kMortonDimsB;
+        int chosen[kMortonDimsB];
+        for (int j = 0; j < m; ++j) {
+            int best = -1;
+            float span = -1.0f;
+            for (int f = 0; f < d; ++f) {
+                bool taken = false;
+                for (int q = 0; q < j; ++q) taken |= chosen[q] == f;
+                const float sp = unflip_f(hi[f]) - unflip_f(lo[f]);
+                if (!taken && sp > span) {
+                    span = sp;
+                    best = f;
+                }
+            }
+            chosen[j] = best;
+            pdims[p * kMortonDimsB + j] = best;
+        }
+    }
+}
+
+// Morton key of each point over its problem's chosen dimensions.
+__global__ void bm_morton_kernel(const float* __restrict__ xc, int64_t ntot, int d, const int* __restrict__ pid,
+                                 const float* __restrict__ pmm, const int* __restrict__ pdims,
+                                 unsigned* __restrict__ keys, unsigned* __restrict__ vals) {
+    for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < ntot;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const int p = pid[i];
+        const int m = d < kMortonDimsB ? d : kMortonDimsB;
+        const int bits = (32 / m) < 10 ? 32 / m : 10;
+        unsigned q[kMortonDimsB];
+        for (int j = 0; j < m; ++j) {
+            const int f = pdims[p * kMortonDimsB + j];
+            const float lo = pmm[(static_cast<int64_t>(p) * d + f) * 2], hi = pmm[(static_cast<int64_t>(p) * d + f) * 2 + 1];
+            const float span = hi - lo;
+            float t = span > 0.0f ? (xc[i * d + f] - lo) / span : 0.0f;
+            t = fminf(fmaxf(t, 0.0f), 1.0f);
+            q[j] = static_cast<unsigned>(t * static_cast<float>((1u << bits) - 1u) + 0.5f);
+        }
+        unsigned key = 0u;
+        for (int bt = bits - 1; bt >= 0; --bt)
+            for (int j = 0; j < m; ++j) key = (key << 1) | ((q[j] >> bt) & 1u);
+        keys[i] = key;
+        vals[i] = static_cast<unsigned>(i);
+    }
+}
+
+__global__ void bm_pidkey_kernel(int64_t ntot, const int* __restrict__ pid, const unsigned* __restrict__ vals,
+                                 unsigned* __restrict__ keys) {
+    for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < ntot;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+        keys[i] = static_cast<unsigned>(pid[vals[i]]);
+}
+
+// Sorted coordinates and, per sorted position, the point's original index
+// within its problem.
+__global__ void bm_gather_kernel(const float* __restrict__ xc, int64_t ntot, int d, const unsigned* __restrict__ perm,
+                                 const int* __restrict__ pid, const int64_t* __restrict__ off, float* __restrict__ xs,
+                                 unsigned* __restrict__ lidx) {
+    for (int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; t < ntot * d;
+         t += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const int64_t i = t / d;
+        const int f = static_cast<int>(t % d);
+        const unsigned src = perm[i];
+        xs[t] = xc[static_cast<int64_t>(src) * d + f];
+        if (f == 0) lidx[i] = static_cast<unsigned>(src - off[pid[src]]);
+    }
+}
+
+// One warp per (problem, tile of 128 sorted points): the tile's bounding box,
+// tbox[tile_off[p] + t][2][d] (lo, hi).
+__global__ void bm_tilebox_kernel(const float* __restrict__ xs, const int64_t* __restrict__ off, int d,
+                                  const int* __restrict__ tpid, const int64_t* __restrict__ toff, int64_t ntiles,
+                                  float* __restrict__ tbox) {
+    const int lane = threadIdx.x & 31;
+    const int64_t g = static_cast<int64_t>(blockIdx.x) * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (g >= ntiles) return;
+    const int p = tpid[g];
+    const int64_t t = g - toff[p];
+    const int64_t b = off[p] + t * kCT;
+    const int64_t e = (b + kCT < off[p + 1]) ? b + kCT : off[p + 1];
+    for (int f = 0; f < d; ++f) {
+        float lo = __int_as_float(0x7f800000), hi = __int_as_float(0xff800000);
+        for (int64_t i = b + lane; i < e; i += 32) {
+            const float v = xs[i * d + f];
+            lo = fminf(lo, v);
+            hi = fmaxf(hi, v);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+            hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+        }
+        if (lane == 0) {
+            tbox[(g * 2) * d + f] = lo;
+            tbox[(g * 2 + 1) * d + f] = hi;
+        }
+    }
+}
+
+// Pruning margin for d <= 64: the float32 direct-difference distance of two
+// points at real squared distance T >= LB is >= T (1 - (d + 2) 2^-24) >
+// LB (1 - 2^-17), so a tile whose rounded-down box gap times (1 - 2^-17)
+// exceeds every row's k-th distance holds no candidate.
+constexpr float kBPruneShrink = 0.9999923706054688f;  // 1 - 2^-17
+
+// Rounded-down squared gap between box a (lo, hi) and box b, lanes over
+// dimensions, round-down sums; the result is warp-uniform.
+__device__ __forceinline__ float gap2_rd(const float* a_lo, const float* a_hi, const float* b_lo, const float* b_hi,
+                                         int d) {
+    const int lane = threadIdx.x & 31;
+    float g = 0.0f;
+    for (int f = lane; f < d; f += 32) {
+        const float gap = fmaxf(0.0f, fmaxf(__fsub_rd(b_lo[f], a_hi[f]), __fsub_rd(a_lo[f], b_hi[f])));
+        g = __fadd_rd(g, __fmul_rd(gap, gap));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) g = __fadd_rd(g, __shfl_xor_sync(0xffffffffu, g, o));
+    return g;
+}
+
 // ---- persistent k-NN ---------------------------------------------------------
 
 template <int DP>
@@ -105,6 +265,10 @@ struct BatchSmem {
     RowLists<kBM> L;
     uint64_t rows2[kRT][DP];         // this item's rows, each coordinate duplicated into both halves
     uint64_t cols2[kCT / 2][DP + 1];  // one column tile as packed column pairs (odd stride)
+    float wbox[kWarps][2][DP];        // each warp's row box
+    float cbox[2][DP];                // the item's row box
+    float tb[2][2][DP];               // column tile box, by tile parity (warp 0 runs at most one tile ahead)
+    int skip_tile[2];
     int item;
 };
 
@@ -147,10 +311,11 @@ __device__ __forceinline__ void offer_row(RowLists<kBM>& L, int r, const uint64_
 // fma.rn).
 template <int DP, int CP>
 __global__ void __launch_bounds__(kThreads)
-batched_knn_kernel(const float* __restrict__ xc, const int64_t* __restrict__ off, const int* __restrict__ ks,
-                   const int64_t* __restrict__ nkoff, const uint2* __restrict__ items, int nitems, int d,
-                   unsigned* __restrict__ counter, int32_t* __restrict__ nbr_idx, float* __restrict__ nbr_d2,
-                   float* __restrict__ kdist2) {
+batched_knn_kernel(const float* __restrict__ xc, const unsigned* __restrict__ lidx, const int64_t* __restrict__ off,
+                   const int* __restrict__ ks, const int64_t* __restrict__ nkoff, const uint2* __restrict__ items,
+                   int nitems, int d, unsigned* __restrict__ counter, int32_t* __restrict__ nbr_idx,
+                   float* __restrict__ nbr_d2, float* __restrict__ kdist2, const float* __restrict__ tbox,
+                   const int64_t* __restrict__ toff) {
     extern __shared__ __align__(16) unsigned char braw[];
     BatchSmem<DP>& sh = *reinterpret_cast<BatchSmem<DP>*>(braw);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -178,8 +343,81 @@ batched_knn_kernel(const float* __restrict__ xc, const int64_t* __restrict__ off
         }
         __syncthreads();
         const int rw = warp * kRowsPerWarp;
+        // row boxes: this warp's 16 rows and (warp 0, after the barrier) the item's
+        {
+            const int r = rw + (lane & 15);
+            const bool rv = r0 + r < n;
+            for (int f = 0; f < d; ++f) {
+                const float v = lo_f(sh.rows2[r][f]);
+                float lo = rv ? v : __int_as_float(0x7f800000), hi = rv ? v : __int_as_float(0xff800000);
+#pragma unroll
+                for (int o = 8; o > 0; o >>= 1) {
+                    lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+                    hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+                }
+                if (lane == 0) {
+                    sh.wbox[warp][0][f] = lo;
+                    sh.wbox[warp][1][f] = hi;
+                }
+            }
+        }
+        __syncthreads();
+        if (tid < d) {
+            float lo = __int_as_float(0x7f800000), hi = __int_as_float(0xff800000);
+            for (int w = 0; w < kWarps; ++w) {
+                lo = fminf(lo, sh.wbox[w][0][tid]);
+                hi = fmaxf(hi, sh.wbox[w][1][tid]);
+            }
+            sh.cbox[0][tid] = lo;
+            sh.cbox[1][tid] = hi;
+        }
+        const unsigned* li = lidx + base;  // original index of each sorted position
+        const int ntp = (n + kCT - 1) / kCT;
+        // column tiles in spiral order from the item's own tile: near points
+        // first, so the lists fill with good neighbours early
 #pragma unroll 1
-        for (int c0 = 0; c0 < n; c0 += kCT) {
+        for (int qt = 0; qt < ntp; ++qt) {
+            const int ct = spiral_tile(T, qt, ntp);
+            const int c0 = ct * kCT;
+            // prune (warp 0): the tile is farther than every row's k-th distance
+            // (bounding boxes only pay in low dimensions: DP <= 8)
+            const int par = qt & 1;
+            if (DP <= 8 && warp == 0) {
+                const float* g = tbox + (toff[p] + ct) * 2 * d;
+                for (int f = lane; f < d; f += 32) {
+                    sh.tb[par][0][f] = g[f];
+                    sh.tb[par][1][f] = g[d + f];
+                }
+                float km = __int_as_float(0xff800000);
+                for (int r = lane; r < kRT; r += 32) {
+                    if (r0 + r < n) {
+                        const uint64_t kk = sh.L.kth[r];
+                        km = fmaxf(km, kk == kKeyMax ? __int_as_float(0x7f800000) : __uint_as_float(key_bits(kk)));
+                    }
+                }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) km = fmaxf(km, __shfl_xor_sync(0xffffffffu, km, o));
+                __syncwarp();
+                const float g2 = gap2_rd(sh.cbox[0], sh.cbox[1], sh.tb[par][0], sh.tb[par][1], d);
+                if (lane == 0) sh.skip_tile[par] = __fmul_rd(g2, kBPruneShrink) > km ? 1 : 0;
+            }
+            if (DP <= 8) {
+                __syncthreads();
+                if (sh.skip_tile[par]) continue;
+            }
+            // this warp's rows may all be beyond the tile
+            bool wskip = false;
+            if (DP <= 8) {
+                float wk = __int_as_float(0xff800000);
+                if (lane < kRowsPerWarp && r0 + rw + lane < n) {
+                    const uint64_t kk = sh.L.kth[rw + lane];
+                    wk = kk == kKeyMax ? __int_as_float(0x7f800000) : __uint_as_float(key_bits(kk));
+                }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) wk = fmaxf(wk, __shfl_xor_sync(0xffffffffu, wk, o));
+                wskip = __fmul_rd(gap2_rd(sh.wbox[warp][0], sh.wbox[warp][1], sh.tb[par][0], sh.tb[par][1], d),
+                                  kBPruneShrink) > wk;
+            }
             // the CTA stages 128 columns (coalesced) as packed pairs
             for (int i = tid; i < kCT * DP; i += kThreads) {
                 const int c = i / DP, f = i % DP;
@@ -188,7 +426,7 @@ batched_knn_kernel(const float* __restrict__ xc, const int64_t* __restrict__ off
             }
             __syncthreads();
 #pragma unroll 1
-            for (int sub = 0; sub < kCT; sub += kTile) {
+            for (int sub = 0; sub < (wskip ? 0 : kCT); sub += kTile) {
             uint64_t cp[CP][DP];
             int cc[CP];
 #pragma unroll
@@ -228,9 +466,9 @@ batched_knn_kernel(const float* __restrict__ xc, const int64_t* __restrict__ off
 #pragma unroll
                     for (int q = 0; q < CP; ++q) {
                         const int ca = cc[q], cb = cc[q] + 1;
-                        key[2 * q] = (gr < n && ca < n && ca != gr) ? make_key(__float_as_uint(lo_f(s[h][q])), ca) : kKeyMax;
+                        key[2 * q] = (gr < n && ca < n && ca != gr) ? make_key(__float_as_uint(lo_f(s[h][q])), li[ca]) : kKeyMax;
                         key[2 * q + 1] =
-                            (gr < n && cb < n && cb != gr) ? make_key(__float_as_uint(hi_f(s[h][q])), cb) : kKeyMax;
+                            (gr < n && cb < n && cb != gr) ? make_key(__float_as_uint(hi_f(s[h][q])), li[cb]) : kKeyMax;
                     }
                     offer_row<CP>(sh.L, r + h, key, k);
                 }
@@ -241,8 +479,8 @@ batched_knn_kernel(const float* __restrict__ xc, const int64_t* __restrict__ off
         // the k best per row, written in the reference's slot order
         for (int rr = 0; rr < kRowsPerWarp; ++rr) {
             const int r = rw + rr;
-            const int il = r0 + r;
-            if (il >= n) break;
+            if (r0 + r >= n) break;
+            const int il = static_cast<int>(li[r0 + r]);  // the row's original index
             compact_row<kBM>(sh.L, r, k, 0.0f, 8);
             const uint64_t kth = sh.L.list[r][k - 1];
             const uint32_t kbits = key_bits(kth);
@@ -331,8 +569,8 @@ void launch_knn_t(int grid, const BatchDev& b, cudaStream_t s) {
                                      static_cast<int>(smem)));
         configured = true;
     }
-    batched_knn_kernel<DP, CP><<<grid, kThreads, smem, s>>>(b.xc, b.off, b.ks, b.nkoff, b.items, b.nitems, b.d,
-                                                           b.counter, b.nbr, b.d2, b.kd);
+    batched_knn_kernel<DP, CP><<<grid, kThreads, smem, s>>>(b.xs, b.lidx, b.off, b.ks, b.nkoff, b.items, b.nitems,
+                                                           b.d, b.counter, b.nbr, b.d2, b.kd, b.tbox, b.toff);
     CG_LAUNCH_CHECK();
 }
 
@@ -383,6 +621,8 @@ void Engine::batch_plan(int num, const int64_t* offsets, const int* ks, int d, b
     P.ks.assign(ks, ks + num);
     P.nkoff.assign(num + 1, 0);
     P.coff.assign(num + 1, 0);
+    P.toff.assign(num + 1, 0);
+    std::vector<int> tp;
     std::vector<std::pair<int64_t, uint2>> items;
     std::vector<int> cp;
     for (int p = 0; p < num; ++p) {
@@ -404,8 +644,11 @@ void Engine::batch_plan(int num, const int64_t* offsets, const int* ks, int d, b
         P.coff[p + 1] = P.coff[p] + chunks;
         for (int64_t c = 0; c < chunks; ++c) cp.push_back(p);
         const int64_t tiles = ceil_div(n, kRT);
-        for (int64_t t = 0; t < tiles; ++t)
+        P.toff[p + 1] = P.toff[p] + tiles;
+        for (int64_t t = 0; t < tiles; ++t) {
             items.push_back({n, make_uint2(static_cast<unsigned>(p), static_cast<unsigned>(t))});
+            tp.push_back(p);
+        }
     }
     // largest problems first: their items are the longest, the tail stays short
     std::stable_sort(items.begin(), items.end(),
@@ -423,6 +666,11 @@ void Engine::batch_plan(int num, const int64_t* offsets, const int* ks, int d, b
     b.ks = bplan_ks_.as<int>(num);
     b.items = bplan_items_.as<uint2>(P.items.size());
     b.cp = bplan_cp_.as<int>(cp.size() ? cp.size() : 1);
+    b.toff = bplan_toff_.as<int64_t>(num + 1);
+    b.tpid = bplan_tpid_.as<int>(tp.size());
+    b.ntiles = static_cast<int64_t>(tp.size());
+    CG_CUDA(cudaMemcpyAsync(b.toff, P.toff.data(), sizeof(int64_t) * (num + 1), cudaMemcpyHostToDevice, s));
+    CG_CUDA(cudaMemcpyAsync(b.tpid, tp.data(), sizeof(int) * tp.size(), cudaMemcpyHostToDevice, s));
     CG_CUDA(cudaMemcpyAsync(b.off, P.off.data(), sizeof(int64_t) * (num + 1), cudaMemcpyHostToDevice, s));
     CG_CUDA(cudaMemcpyAsync(b.nkoff, P.nkoff.data(), sizeof(int64_t) * (num + 1), cudaMemcpyHostToDevice, s));
     CG_CUDA(cudaMemcpyAsync(b.coff, P.coff.data(), sizeof(int64_t) * (num + 1), cudaMemcpyHostToDevice, s));
@@ -442,6 +690,14 @@ void Engine::batch_plan(int num, const int64_t* offsets, const int* ks, int d, b
     b.kd = bkd_.as<float>(P.ntot);
     b.lrd = blrd_.as<float>(P.ntot);
     b.counter = bcounter_.as<unsigned>(1);
+    b.xs = bxs_.as<float>(static_cast<size_t>(P.ntot) * d);
+    b.lidx = blidx_.as<unsigned>(P.ntot);
+    b.pmm = bpmm_.as<float>(static_cast<size_t>(num) * d * 2);
+    b.pdims = bpdims_.as<int>(static_cast<size_t>(num) * kMortonDimsB);
+    b.skeys = bskeys_.as<unsigned>(2 * static_cast<size_t>(P.ntot));
+    b.svals = bsvals_.as<unsigned>(2 * static_cast<size_t>(P.ntot));
+    b.scounts = bscounts_.as<unsigned>(sort_pairs_counts(P.ntot));
+    b.tbox = btbox_.as<float>(static_cast<size_t>(b.ntiles) * 2 * d);
     pid_kernel<<<num < 4096 ? num : 4096, 256, 0, s>>>(b.off, num, b.pid);
     CG_LAUNCH_CHECK();
     CG_CUDA(cudaStreamSynchronize(s));
@@ -470,6 +726,27 @@ void Engine::batch_launch(const float* d_x, float* d_scores) {
         CG_LAUNCH_CHECK();
     }
     bc_apply_kernel<<<grid_cap(P.ntot * d), 256, 0, s>>>(d_x, P.ntot, d, b.pid, b.mean, b.inv, b.xc);
+    CG_LAUNCH_CHECK();
+    // spatial order within each problem: Morton keys, stable sort by key,
+    // then stable sort by problem (keeps each problem's range in place)
+    bm_minmax_kernel<<<P.num, 256, 0, s>>>(b.xc, b.off, d, b.pmm, b.pdims);
+    CG_LAUNCH_CHECK();
+    bm_morton_kernel<<<grid_cap(P.ntot), 256, 0, s>>>(b.xc, P.ntot, d, b.pid, b.pmm, b.pdims, b.skeys, b.svals);
+    CG_LAUNCH_CHECK();
+    unsigned* vs = nullptr;
+    unsigned* ks1 = sort_pairs_stable(b.skeys, b.svals, b.skeys + P.ntot, b.svals + P.ntot, P.ntot, 32, b.scounts, s, &vs);
+    unsigned* kother = ks1 == b.skeys ? b.skeys + P.ntot : b.skeys;
+    unsigned* vother = vs == b.svals ? b.svals + P.ntot : b.svals;
+    bm_pidkey_kernel<<<grid_cap(P.ntot), 256, 0, s>>>(P.ntot, b.pid, vs, ks1);
+    CG_LAUNCH_CHECK();
+    int pbits = 8;
+    while (pbits < 32 && (static_cast<int64_t>(1) << pbits) < P.num) pbits += 8;
+    unsigned* perm = nullptr;
+    sort_pairs_stable(ks1, vs, kother, vother, P.ntot, pbits, b.scounts, s, &perm);
+    bm_gather_kernel<<<grid_cap(P.ntot * d), 256, 0, s>>>(b.xc, P.ntot, d, perm, b.pid, b.off, b.xs, b.lidx);
+    CG_LAUNCH_CHECK();
+    bm_tilebox_kernel<<<static_cast<unsigned>(ceil_div(b.ntiles, 8)), 256, 0, s>>>(b.xs, b.off, d, b.tpid, b.toff,
+                                                                                   b.ntiles, b.tbox);
     CG_LAUNCH_CHECK();
     CG_CUDA(cudaMemsetAsync(b.counter, 0, sizeof(unsigned), s));
     launch_knn(dp_for(d), btune_packed_, btune_grid_, b, s);

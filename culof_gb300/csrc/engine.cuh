@@ -37,7 +37,7 @@ struct BatchPlan {
     int num = 0;
     int d = 0;
     bool normalize = false;
-    std::vector<int64_t> off, nkoff, coff;  // points, k-NN slots, centring chunks per problem (prefix sums)
+    std::vector<int64_t> off, nkoff, coff, toff;  // points, k-NN slots, centring chunks, row tiles (prefix sums)
     std::vector<int> ks;
     std::vector<uint2> items;  // (problem, row tile), largest problems first
     int64_t ntot = 0, nchunks = 0;
@@ -54,6 +54,17 @@ struct BatchDev {
     int32_t* nbr = nullptr;
     float *d2 = nullptr, *kd = nullptr, *lrd = nullptr;
     unsigned* counter = nullptr;
+    // spatial order: sorted coordinates, original index of each sorted point
+    float* xs = nullptr;
+    unsigned* lidx = nullptr;
+    float* pmm = nullptr;
+    int* pdims = nullptr;
+    unsigned *skeys = nullptr, *svals = nullptr, *scounts = nullptr;
+    // tiles of 128 sorted points: problem, first tile per problem, boxes
+    int* tpid = nullptr;
+    int64_t* toff = nullptr;
+    int64_t ntiles = 0;
+    float* tbox = nullptr;
 };
 
 enum Path : int { kPathAuto = 0, kPathFast = 1, kPathGeneral = 2, kPathTensor = 3 };
@@ -128,6 +139,8 @@ private:
     BatchDev bdev_;
     DevBuf bplan_off_, bplan_nkoff_, bplan_coff_, bplan_ks_, bplan_items_, bplan_cp_;
     DevBuf bpid_, bxc_, bpartial_, bmean_, binv_, bnbr_, bd2_, bkd_, blrd_, bcounter_;
+    DevBuf bxs_, blidx_, bpmm_, bpdims_, bskeys_, bsvals_, bscounts_;
+    DevBuf bplan_toff_, bplan_tpid_, btbox_;
     bool use_graphs_ = true;
     bool btuned_ = false, btune_packed_ = true, bbest_packed_ = true;
     int btune_grid_ = 152, bbest_grid_ = 152;
