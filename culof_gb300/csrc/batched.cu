@@ -429,13 +429,19 @@ batched_knn_kernel(const float* __restrict__ xc, const unsigned* __restrict__ li
             for (int sub = 0; sub < (wskip ? 0 : kCT); sub += kTile) {
             uint64_t cp[CP][DP];
             int cc[CP];
+            // per column: its original index in the key's low half, or all
+            // ones (a key of kKeyMax) for columns beyond the problem
+            uint64_t cidx[2 * CP];
 #pragma unroll
             for (int q = 0; q < CP; ++q) {
                 const int pr = (sub >> 1) + 32 * q + lane;  // column pair index in the tile
                 cc[q] = c0 + 2 * pr;
 #pragma unroll
                 for (int f = 0; f < DP; ++f) cp[q][f] = sh.cols2[pr][f];
+                cidx[2 * q] = cc[q] < n ? static_cast<uint64_t>(li[cc[q]]) : kKeyMax;
+                cidx[2 * q + 1] = cc[q] + 1 < n ? static_cast<uint64_t>(li[cc[q] + 1]) : kKeyMax;
             }
+            const bool own = c0 == r0;  // the only tile holding the rows' own points
 #pragma unroll 1
             for (int rr = 0; rr < kRowsPerWarp; rr += 2) {
                 const int r = rw + rr;
@@ -462,13 +468,16 @@ batched_knn_kernel(const float* __restrict__ xc, const unsigned* __restrict__ li
 #pragma unroll
                 for (int h = 0; h < 2; ++h) {
                     const int gr = r0 + r + h;
+                    if (gr >= n) break;  // warp-uniform
                     uint64_t key[2 * CP];
 #pragma unroll
                     for (int q = 0; q < CP; ++q) {
-                        const int ca = cc[q], cb = cc[q] + 1;
-                        key[2 * q] = (gr < n && ca < n && ca != gr) ? make_key(__float_as_uint(lo_f(s[h][q])), li[ca]) : kKeyMax;
-                        key[2 * q + 1] =
-                            (gr < n && cb < n && cb != gr) ? make_key(__float_as_uint(hi_f(s[h][q])), li[cb]) : kKeyMax;
+                        key[2 * q] = (static_cast<uint64_t>(__float_as_uint(lo_f(s[h][q]))) << 32) | cidx[2 * q];
+                        key[2 * q + 1] = (static_cast<uint64_t>(__float_as_uint(hi_f(s[h][q]))) << 32) | cidx[2 * q + 1];
+                        if (own) {  // a row is not its own neighbour
+                            if (cc[q] == gr) key[2 * q] = kKeyMax;
+                            if (cc[q] + 1 == gr) key[2 * q + 1] = kKeyMax;
+                        }
                     }
                     offer_row<CP>(sh.L, r + h, key, k);
                 }
