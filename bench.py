@@ -53,6 +53,14 @@ L2_FLUSH_BYTES = 256 << 20
 
 PATH_NAMES = ["auto", "fast", "general", "tensor"]
 
+# DRAM traffic of one sweep_kernel launch, measured by one ncu capture of this
+# very workload (dram__bytes_read.sum + dram__bytes_write.sum); other
+# workloads report null.
+MEASURED_SWEEP_TRAFFIC = {
+    ("clusters", 200_000, 8, 20): (18_867_712 + 76_127_488,
+                                   "ncu: 18.9 MB read + 76.1 MB written per sweep_kernel launch at this workload"),
+}
+
 
 def tensor_peak():
     """Dense 16-bit tensor peak: the measured cuBLAS bf16 burst figure (f16
@@ -409,6 +417,7 @@ def run_ours(args):
         # efficiency on those is reported beside it
         achieved = 2.0 * d * sweep_pairs / (sweep_ms * 1e-3) / 1e12
         executed = 2.0 * d * (ev_pairs if unpruned_pairs > 0 else sweep_pairs) / (sweep_ms * 1e-3) / 1e12
+        traffic, traffic_src = MEASURED_SWEEP_TRAFFIC.get((args.workload, n, d, k), (None, None))
         roofline = {
             "bound": "fp32",
             "kernel": "sweep_kernel (fused distance + filtered exact select)",
@@ -416,7 +425,7 @@ def run_ours(args):
             "peak": fp32_peak,
             "unit": "TFLOP/s",
             "frac": achieved / fp32_peak,
-            "traffic": None,
+            "traffic": traffic,
             "peak_source": "measured FP32 FMA throughput (culof_probe_fp32_tflops, best of scalar/packed)",
             "algorithmic_flop_per_pair": 2 * d,
             "pairs_per_launch": sweep_pairs,
@@ -424,6 +433,7 @@ def run_ours(args):
             "pruned_fraction": (1.0 - ev_pairs / unpruned_pairs) if unpruned_pairs > 0 else 0.0,
             "executed_tflops": executed,
             "executed_frac": executed / fp32_peak,
+            "traffic_source": traffic_src,
             "sweep_share_of_step": sweep_ms / mean_ms,
         }
     cpu = None
