@@ -154,7 +154,7 @@ private:
     DevBuf morton_, perm_, sort_tmp_, sort_hist_, cols_, rows_, tc_lists_;
     // the FP32 sweep's evaluated (warp x column tile) blocks; the total it
     // would evaluate without pruning
-    DevBuf pair_stats_, boxes_, plist_, pcount_;
+    DevBuf pair_stats_, boxes_, plist_, pcount_, order_;
     unsigned long long stat_total_blocks_ = 0;
     // Device status word of the current call: kernels set it (a bounded wait
     // that expired, an out-of-range neighbour index); host paths check it.

@@ -376,6 +376,16 @@ __device__ __forceinline__ float box_gap2_rd(const float* __restrict__ a_lo, con
     return __shfl_sync(0xffffffffu, g, 0);
 }
 
+// Keys for the launch order of the sweep: 0xFFFF - list length (ascending
+// sort = longest lists first), values the row tiles.
+__global__ void order_key_kernel(const int* __restrict__ pcount, int nt, unsigned* __restrict__ keys,
+                                 unsigned* __restrict__ vals) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nt) return;
+    keys[t] = 0xFFFFu - static_cast<unsigned>(pcount[t]);
+    vals[t] = static_cast<unsigned>(t);
+}
+
 // Per row tile T (one block): the column tiles that can hold a candidate for
 // any of its rows under the seed's k-th distances, in the sweep's visiting
 // order, each with its rounded-down box gap (the sweep re-tests the gap
@@ -541,11 +551,15 @@ __global__ void __launch_bounds__(kThreads, 2)
 sweep_kernel(const float* __restrict__ tiles, int nt, int nsplit, int k, const unsigned* __restrict__ max_norm_bits,
              unsigned long long* __restrict__ kth_shared, uint64_t* __restrict__ partial, int* __restrict__ status,
              unsigned long long* __restrict__ evaluated_blocks, const uint2* __restrict__ plist,
-             const int* __restrict__ pcount) {
+             const int* __restrict__ pcount, const unsigned* __restrict__ order) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     SweepSmem<DP, M>& sh = *reinterpret_cast<SweepSmem<DP, M>*>(smem_raw);
-    const int T = blockIdx.x % nt;
-    const int split = blockIdx.x / nt;
+    // row tiles with the longest candidate lists first (tail balance)
+    // (split-major: a row tile's later splits start after its earlier ones
+    // have shared their k-th keys, so they prune more)
+    const int ti = static_cast<int>(blockIdx.x) % nt;
+    const int T = order ? static_cast<int>(order[ti]) : ti;
+    const int split = static_cast<int>(blockIdx.x) / nt;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const float nmax = __uint_as_float(*max_norm_bits);
     const float* own = tiles + static_cast<int64_t>(T) * tile_floats(DP);
@@ -916,7 +930,7 @@ namespace {
 template <int DP, int M>
 void launch_sweep(const float* tiles, int nt, int nsplit, int k, const unsigned* maxn, unsigned long long* kth_shared,
                   uint64_t* partial, int* status, unsigned long long* evaluated, const uint2* plist, const int* pcount,
-                  cudaStream_t s) {
+                  const unsigned* order, cudaStream_t s) {
     const size_t smem = sizeof(SweepSmem<DP, M>);
     static bool configured = false;  // per instantiation; the attribute is set once per process
     if (!configured) {
@@ -925,7 +939,7 @@ void launch_sweep(const float* tiles, int nt, int nsplit, int k, const unsigned*
         configured = true;
     }
     sweep_kernel<DP, M><<<nt * nsplit, kThreads, smem, s>>>(tiles, nt, nsplit, k, maxn, kth_shared, partial, status,
-                                                            evaluated, plist, pcount);
+                                                            evaluated, plist, pcount, order);
     CG_LAUNCH_CHECK();
 }
 
@@ -1083,6 +1097,7 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
     // 3b. per row tile: the column tiles the seed's k-th distances leave
     uint2* plist = nullptr;
     int* pcount = nullptr;
+    const unsigned* order = nullptr;
     constexpr int kMaxListTiles = 16384;  // lists take nt^2 x 8 bytes: up to 2 GiB
     if (!wide && !tensor && nt > 1 && nt <= kMaxListTiles) {
         plist = plist_.as<uint2>(static_cast<size_t>(nt) * nt);
@@ -1094,6 +1109,14 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
             default: prune_list_kernel<8><<<nt, 256, 0, s>>>(boxes, nt, kth_shared, plist, pcount); break;
         }
         CG_LAUNCH_CHECK();
+        // launch order: longest lists first
+        unsigned* ok = reinterpret_cast<unsigned*>(order_.get(sizeof(unsigned) * (4 * static_cast<size_t>(nt) +
+                                                                                   sort_pairs_counts(nt))));
+        order_key_kernel<<<grid_for(nt, 256), 256, 0, s>>>(pcount, nt, ok, ok + nt);
+        CG_LAUNCH_CHECK();
+        unsigned* sorted_vals = nullptr;
+        sort_pairs_stable(ok, ok + nt, ok + 2 * nt, ok + 3 * nt, nt, 16, ok + 4 * nt, s, &sorted_vals);
+        order = sorted_vals;
     }
 
     // 4. sweep over the other tiles, split S ways
@@ -1108,8 +1131,10 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
     } else if (nt > 1) {
         const bool big = k > 32;
 #define CG_SWEEP(DPV)                                                                                 \
-    (big ? launch_sweep<DPV, 96>(tiles, nt, nsplit, k, maxn, kth_shared, partial, status, evaluated, plist, pcount, s) \
-         : launch_sweep<DPV, 64>(tiles, nt, nsplit, k, maxn, kth_shared, partial, status, evaluated, plist, pcount, s))
+    (big ? launch_sweep<DPV, 96>(tiles, nt, nsplit, k, maxn, kth_shared, partial, status, evaluated, plist, pcount, \
+                                 order, s)                                                                         \
+         : launch_sweep<DPV, 64>(tiles, nt, nsplit, k, maxn, kth_shared, partial, status, evaluated, plist, pcount, \
+                                 order, s))
         switch (dp) {
             case 2: CG_SWEEP(2); break;
             case 4: CG_SWEEP(4); break;
