@@ -108,6 +108,36 @@ def lof(X: ArrayLike, k: int = 20, normalize: bool = False) -> NDArray[np.float3
     return scores
 
 
+def lof_batched(problems, k=20, normalize: bool = False) -> list:
+    """LOF of many independent problems in one GPU call (an extension: the
+    reference computes one problem per call).
+
+    Parameters
+    ----------
+    problems : sequence of array-likes, each of shape (n_i, n_features)
+        The same number of features in every problem.
+    k : int or sequence of int, default=20
+        Neighbours per point, one value for all problems or one per problem;
+        each ``1 <= k_i <= n_i - 1`` and ``k_i <= 48``.
+    normalize : bool, default=False
+        Z-score each feature of each problem before computing distances.
+
+    Returns
+    -------
+    list of ndarray
+        Each problem's scores, bit-identical to ``lof(problem, k_i)``.
+    """
+    arrs = list(problems)
+    ks = [int(k)] * len(arrs) if np.ndim(k) == 0 else [int(v) for v in k]
+    if len(ks) != len(arrs):
+        raise ValueError("k must be one value or one value per problem")
+    checked = [_validate(X, ki) for X, ki in zip(arrs, ks)]
+    out = _culof.lof_batched(checked, ks, normalize)
+    for scores in out:
+        _check_finite_scores(scores)
+    return out
+
+
 class LOF:
     """Unsupervised outlier detection with Local Outlier Factor, on the GPU.
 

@@ -78,6 +78,8 @@ _SIGS = {
     "culof_context_lof_backward_device": ([_P, _P, _I64, _I, _I, _I, _P, _P, _P, _P], _I),
     "culof_context_lof_batched_device": ([_P, _I, _P, _P, _P, _I, _I, _P], _I),
     "culof_context_set_graphs": ([_P, _I], _I),
+    "culof_lof_batched": ([_I, _P, _P, _P, _I, _I, _P], _I),
+    "culof_context_lof_batched": ([_P, _I, _P, _P, _P, _I, _I, _P], _I),
     "culof_context_pair_stats": ([_P, ctypes.POINTER(_D), ctypes.POINTER(_D)], _I),
     "culof_compute_scores": ([_P, _P, _P, _I64, _I, _P], _I),
     "culof_context_contamination_offset_device": ([_P, _P, _I64, _D, _P], _I),
@@ -146,6 +148,27 @@ def fit_predict(points, k: int, normalize: bool, contamination):
         )
     )
     return nof, labels, off.value
+
+
+def lof_batched(problems, ks, normalize: bool) -> list:
+    """Raw LOF scores of many independent problems (each (n_i, d) float32,
+    one k per problem) in one GPU call; a list of float32 arrays."""
+    arrs = [_as_points(p) for p in problems]
+    if not arrs:
+        return []
+    d = arrs[0].shape[1]
+    if any(a.shape[1] != d for a in arrs):
+        raise ValueError("every problem must have the same number of features")
+    kk = np.ascontiguousarray(ks, dtype=np.int32)
+    if kk.shape != (len(arrs),):
+        raise ValueError("one k per problem")
+    off = np.zeros(len(arrs) + 1, np.int64)
+    off[1:] = np.cumsum([a.shape[0] for a in arrs])
+    X = np.ascontiguousarray(np.concatenate(arrs), dtype=np.float32)
+    out = np.empty(X.shape[0], np.float32)
+    _check(_lib.culof_lof_batched(len(arrs), off.ctypes.data, kk.ctypes.data, X.ctypes.data, d,
+                                  int(bool(normalize)), out.ctypes.data))
+    return [out[off[i]:off[i + 1]].copy() for i in range(len(arrs))]
 
 
 def contamination_offset_noalloc(stream: int, nof: int, n_points: int, contamination, offset: int) -> None:

@@ -267,6 +267,21 @@ int culof_context_lof_batched_device(culof_context* ctx, int num_problems, const
     });
 }
 
+int culof_lof_batched(int num_problems, const int64_t* offsets, const int* ks, const float* points, int n_dims,
+                      int normalize, float* scores_out) {
+    return guarded([&] {
+        require_device();
+        thread_engine().lof_batched_host(num_problems, offsets, ks, points, n_dims, normalize != 0, scores_out);
+    });
+}
+
+int culof_context_lof_batched(culof_context* ctx, int num_problems, const int64_t* offsets, const int* ks,
+                              const float* points, int n_dims, int normalize, float* scores_out) {
+    return guarded([&] {
+        engine_of(ctx).lof_batched_host(num_problems, offsets, ks, points, n_dims, normalize != 0, scores_out);
+    });
+}
+
 int culof_context_set_graphs(culof_context* ctx, int on) {
     return guarded([&] { engine_of(ctx).set_graphs(on != 0); });
 }

@@ -852,4 +852,19 @@ void Engine::lof_batched_device(int num, const int64_t* offsets, const int* ks, 
     count_launches(bgraph_kernels_);
 }
 
+void Engine::lof_batched_host(int num, const int64_t* offsets, const int* ks, const float* x, int d, bool normalize,
+                              float* scores) {
+    if (!x || !scores) throw Error(kInvalidArgument, "points and scores must not be null");
+    if (num < 1 || !offsets) throw Error(kInvalidArgument, "num_problems must be >= 1");
+    CG_CUDA(cudaSetDevice(device_));
+    const int64_t ntot = offsets[num];
+    if (ntot < 0) throw Error(kInvalidArgument, "offsets must be non-decreasing");
+    float* dx = x_.as<float>(static_cast<size_t>(ntot) * (d > 0 ? d : 1));
+    float* ds = scores_.as<float>(static_cast<size_t>(ntot > 0 ? ntot : 1));
+    CG_CUDA(cudaMemcpyAsync(dx, x, sizeof(float) * ntot * d, cudaMemcpyHostToDevice, stream_));
+    lof_batched_device(num, offsets, ks, dx, d, normalize, ds);
+    CG_CUDA(cudaMemcpyAsync(scores, ds, sizeof(float) * ntot, cudaMemcpyDeviceToHost, stream_));
+    check_status();
+}
+
 }  // namespace culof_gb300

@@ -101,6 +101,8 @@ public:
     // CUDA graph while the batch layout and pointers repeat.
     void lof_batched_device(int num, const int64_t* offsets, const int* ks, const float* d_x, int d, bool normalize,
                             float* d_scores);
+    void lof_batched_host(int num, const int64_t* offsets, const int* ks, const float* x, int d, bool normalize,
+                          float* scores);
     void set_graphs(bool on) { use_graphs_ = on; }
     // Pairs the last FP32 small-d sweep evaluated and the pairs of an
     // unpruned sweep (both 0 for other paths); synchronises.

@@ -95,7 +95,7 @@ bf16_gram_tile_kernel(const __grid_constant__ CUtensorMap ta, const __grid_const
                 const int half = k >> 2, sub = k & 3;
                 const uint64_t ad = sw128_desc(smem_u32(sh.a[half]) + 32 * sub);
                 const uint64_t bd = sw128_desc(smem_u32(sh.b[half]) + 32 * sub);
-                mma_bf16(tmem, ad, bd, idesc, k > 0);
+                mma_f16kind(tmem, ad, bd, idesc, k > 0);
             }
             mma_commit(&sh.mma_bar);
         }

@@ -73,8 +73,10 @@ __device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
-// D[tmem] (+)= A * B^T, one elected thread.
-__device__ __forceinline__ void mma_bf16(uint32_t tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc, bool accumulate) {
+// D[tmem] (+)= A * B^T for 16-bit operands (kind::f16: f16 or bf16, as the
+// instruction descriptor says), one elected thread.
+__device__ __forceinline__ void mma_f16kind(uint32_t tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                            bool accumulate) {
     asm volatile(
         "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
             tmem),

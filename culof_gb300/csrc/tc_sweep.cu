@@ -601,7 +601,7 @@ tc_sweep_kernel(const __grid_constant__ CUtensorMap tmap, const float* __restric
                     const int kb = kk >> 2, sub = kk & 3;
                     const uint64_t ad = tc::sw128_desc(smem_u32(sh.a[kb]) + 32 * sub);
                     const uint64_t bd = tc::sw128_desc(smem_u32(sh.b[s][kb]) + 32 * sub);
-                    tc::mma_bf16(dt, ad, bd, idesc, kk > 0);
+                    tc::mma_f16kind(dt, ad, bd, idesc, kk > 0);
                 }
                 tc::mma_commit(&sh.empty[s]);
                 tc::mma_commit(&sh.tfull[acc]);

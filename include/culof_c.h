@@ -170,6 +170,12 @@ CULOF_API int culof_compute_scores(void* cuda_stream, const int32_t* d_nbr_idx, 
 CULOF_API int culof_context_lof_batched_device(culof_context* ctx, int num_problems, const int64_t* offsets,
                                                const int* ks, const float* d_points, int n_dims, int normalize,
                                                float* d_scores);
+/* The same on host arrays: copies in, runs, copies out, synchronises
+ * (points and scores_out host, offsets and ks as above). */
+CULOF_API int culof_lof_batched(int num_problems, const int64_t* offsets, const int* ks, const float* points,
+                                int n_dims, int normalize, float* scores_out);
+CULOF_API int culof_context_lof_batched(culof_context* ctx, int num_problems, const int64_t* offsets, const int* ks,
+                                        const float* points, int n_dims, int normalize, float* scores_out);
 /* Graph capture of repeated batched calls: on (1, default) or off (0). */
 CULOF_API int culof_context_set_graphs(culof_context* ctx, int on);
 

@@ -121,3 +121,17 @@ def test_batched_config4_subset_bit_exact():
         rng = np.random.default_rng(2)
         for i in rng.choice(len(probs), 24, replace=False):
             np.testing.assert_array_equal(got[i].view(np.uint32), ctx.lof(probs[i], ks[i]).view(np.uint32))
+
+
+def test_package_lof_batched_host_arrays():
+    import culof_gb300
+
+    probs, ks = synthetic.batched_problems(12, 16, seed=11, n_range=(128, 2000))
+    got = culof_gb300.lof_batched(probs, ks)
+    for p, k, g in zip(probs, ks, got):
+        np.testing.assert_array_equal(g, culof_gb300.lof(p, k))
+    same_k = culof_gb300.lof_batched(probs[:3], 15)
+    for p, g in zip(probs[:3], same_k):
+        np.testing.assert_array_equal(g, culof_gb300.lof(p, 15))
+    with pytest.raises(ValueError):
+        culof_gb300.lof_batched(probs[:2], [10])

@@ -80,7 +80,8 @@ KNN_CASES = [
     ("d100_k40", lambda: synthetic.reference_test_data(2500, 100, seed=27, n_outliers=25), 40),
     ("factor_d128_k50", lambda: synthetic.factor_model(3000, 128, seed=28), 50),
     # 10,000 points on 50 positions: every point has 199 exact duplicates,
-    # which drives list overflows and the exact re-run of a block
+    # which keeps the lists full of exact ties (and, on the tensor path,
+    # drives rows into exact-key lists)
     ("dups_heavy", lambda: np.repeat(np.random.default_rng(5).uniform(-3, 3, (50, 4)).astype(np.float32), 200,
                                      axis=0)[np.random.default_rng(6).permutation(10_000)], 20),
 ]
