@@ -1109,7 +1109,10 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
             default: prune_list_kernel<8><<<nt, 256, 0, s>>>(boxes, nt, kth_shared, plist, pcount); break;
         }
         CG_LAUNCH_CHECK();
-        // launch order: longest lists first
+    }
+    // launch order: longest lists first (balances the tail of a many-wave
+    // grid; small grids skip the sort)
+    if (plist && nt >= 4 * sms) {
         unsigned* ok = reinterpret_cast<unsigned*>(order_.get(sizeof(unsigned) * (4 * static_cast<size_t>(nt) +
                                                                                    sort_pairs_counts(nt))));
         order_key_kernel<<<grid_for(nt, 256), 256, 0, s>>>(pcount, nt, ok, ok + nt);
