@@ -572,12 +572,7 @@ int dp_for(int d) { return d <= 4 ? 4 : d <= 8 ? 8 : d <= 16 ? 16 : d <= 32 ? 32
 template <int DP, int CP>
 void launch_knn_t(int grid, const BatchDev& b, cudaStream_t s) {
     const size_t smem = sizeof(BatchSmem<DP>);
-    static bool configured = false;
-    if (!configured) {
-        CG_CUDA(cudaFuncSetAttribute(batched_knn_kernel<DP, CP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     static_cast<int>(smem)));
-        configured = true;
-    }
+    set_max_dynamic_smem(reinterpret_cast<const void*>(batched_knn_kernel<DP, CP>), static_cast<int>(smem));
     batched_knn_kernel<DP, CP><<<grid, kThreads, smem, s>>>(b.xs, b.lidx, b.off, b.ks, b.nkoff, b.items, b.nitems,
                                                            b.d, b.counter, b.nbr, b.d2, b.kd, b.tbox, b.toff);
     CG_LAUNCH_CHECK();

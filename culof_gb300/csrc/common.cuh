@@ -44,6 +44,10 @@ void uncount_launches(unsigned long long n);
         CG_CUDA(cudaGetLastError());       \
     } while (0)
 
+// Raise a kernel's dynamic shared-memory limit on the current device, once
+// per (kernel, device) in the process (engine.cu).
+void set_max_dynamic_smem(const void* kernel, int bytes);
+
 // Selection keys: (squared-distance bits << 32) | original column index.
 // Squared distances are never negative (and never -0.0), so their IEEE bit
 // patterns order like the values; the index breaks ties in ascending order.

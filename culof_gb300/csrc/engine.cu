@@ -4,7 +4,10 @@
 // no cuBLAS, and a fused k-NN path whose n x n distances never reach HBM.
 #include <atomic>
 #include <cstdlib>
+#include <mutex>
+#include <set>
 #include <sstream>
+#include <utility>
 
 #include "engine.cuh"
 #include "fast.cuh"
@@ -20,6 +23,17 @@ void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 void count_launches(unsigned long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 void uncount_launches(unsigned long long n) { g_launches.fetch_sub(n, std::memory_order_relaxed); }
 unsigned long long launch_count() { return g_launches.load(std::memory_order_relaxed); }
+
+void set_max_dynamic_smem(const void* kernel, int bytes) {
+    static std::mutex mu;
+    static std::set<std::pair<std::pair<const void*, int>, int>> done;  // ((kernel, device), bytes)
+    int dev = 0;
+    CG_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lock(mu);
+    if (done.count({{kernel, dev}, bytes})) return;
+    CG_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+    done.insert({{kernel, dev}, bytes});
+}
 
 void throw_cuda(cudaError_t err, const char* file, int line, const char* expr) {
     std::ostringstream os;

@@ -932,12 +932,7 @@ void launch_sweep(const float* tiles, int nt, int nsplit, int k, const unsigned*
                   uint64_t* partial, int* status, unsigned long long* evaluated, const uint2* plist, const int* pcount,
                   const unsigned* order, cudaStream_t s) {
     const size_t smem = sizeof(SweepSmem<DP, M>);
-    static bool configured = false;  // per instantiation; the attribute is set once per process
-    if (!configured) {
-        CG_CUDA(cudaFuncSetAttribute(sweep_kernel<DP, M>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     static_cast<int>(smem)));
-        configured = true;
-    }
+    set_max_dynamic_smem(reinterpret_cast<const void*>(sweep_kernel<DP, M>), static_cast<int>(smem));
     sweep_kernel<DP, M><<<nt * nsplit, kThreads, smem, s>>>(tiles, nt, nsplit, k, maxn, kth_shared, partial, status,
                                                             evaluated, plist, pcount, order);
     CG_LAUNCH_CHECK();

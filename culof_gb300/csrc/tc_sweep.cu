@@ -831,11 +831,7 @@ TcBuffers tc_prepare(void* buf, const float* xc, const float* norms, int64_t n, 
 void tc_seed(const TcBuffers& b, int nt, int d, int k, uint64_t* seed_keys, unsigned long long* kth_shared,
              cudaStream_t s) {
     const size_t smem = sizeof(float) * (static_cast<size_t>(kCT) * (b.dr + 1) + kCT);
-    static bool configured = false;
-    if (!configured) {
-        CG_CUDA(cudaFuncSetAttribute(tc_seed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
-        configured = true;
-    }
+    set_max_dynamic_smem(reinterpret_cast<const void*>(tc_seed_kernel), 100 * 1024);
     tc_seed_kernel<<<nt, 256, smem, s>>>(b.xr, b.ix, d, b.dr, k, seed_keys, kth_shared);
     CG_LAUNCH_CHECK();
 }
@@ -843,12 +839,7 @@ void tc_seed(const TcBuffers& b, int nt, int d, int k, uint64_t* seed_keys, unsi
 void tc_sweep(const TcBuffers& b, int nt, int nsplit, int d, int k, const unsigned* maxn,
               unsigned long long* kth_shared, uint64_t* partial, uint64_t* lists, int* status, cudaStream_t s) {
     const size_t smem = sizeof(TcSmem) + 1024;
-    static bool configured = false;
-    if (!configured) {
-        CG_CUDA(cudaFuncSetAttribute(tc_sweep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     static_cast<int>(smem)));
-        configured = true;
-    }
+    set_max_dynamic_smem(reinterpret_cast<const void*>(tc_sweep_kernel), static_cast<int>(smem));
     const CUtensorMap map = tc::make_kmajor_map(b.xh, static_cast<int64_t>(nt) * kCT, b.Kp, true);
     // row tiles in batches, so that the list workspace stays bounded
     const int ntb_max = kTcMaxCtasPerLaunch / nsplit > 0 ? kTcMaxCtasPerLaunch / nsplit : 1;
