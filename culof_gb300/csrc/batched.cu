@@ -338,6 +338,7 @@ batched_knn_kernel(const float* __restrict__ xc, const unsigned* __restrict__ li
         }
         if (tid < kRT) {
             sh.L.cnt[tid] = 0;
+            sh.L.sorted[tid] = 0;
             sh.L.kth[tid] = kKeyMax;
             sh.L.row_norm[tid] = 0.0f;
         }

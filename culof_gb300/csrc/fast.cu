@@ -582,6 +582,7 @@ sweep_kernel(const float* __restrict__ tiles, int nt, int nsplit, int k, const u
                           ? __int_as_float(0xff800000)
                           : tau_from(kk, nr, nmax, DP);
         sh.L.cnt[tid] = 0;
+        sh.L.sorted[tid] = 0;
 #pragma unroll
         for (int f = 0; f < DP; ++f) {
             sh.rowc[tid][f] = tile_coord<DP>(own, tid, f);

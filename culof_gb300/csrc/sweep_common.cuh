@@ -125,12 +125,33 @@ struct RowLists {
     float tau[kRT];
     float row_norm[kRT];
     int cnt[kRT];
+    int sorted[kRT];  // list[r][0..sorted) is sorted and unique (the last compaction's result)
 };
 
 // Compact row r's list (whole warp): sort, drop duplicates, keep the k
 // smallest; tighten the row's k-th key (only downwards) and its threshold.
 template <int M>
 __device__ void compact_row(RowLists<M>& L, int r, int k, float nmax, int dp) {
+    if constexpr (M > 64) {
+        // fast form for lists the full network sorts as 128 keys: sort only
+        // the entries added since the last compaction (at most 64) and merge
+        // them with its sorted result
+        const int c = min(L.cnt[r], M), s = L.sorted[r];
+        if (s >= 0 && s <= c && s <= 128 && c - s <= 64) {
+            uint64_t kk;
+            const int kept = merge_sorted_prefix(L.list[r], s, c, k, k - 1, [](uint64_t) { return kKeyMax; }, &kk);
+            if ((threadIdx.x & 31) == 0) {
+                L.cnt[r] = kept;
+                L.sorted[r] = kept;
+                if (kk != kKeyMax && kk < L.kth[r]) {
+                    L.kth[r] = kk;
+                    L.tau[r] = tau_from(kk, L.row_norm[r], nmax, dp);
+                }
+            }
+            __syncwarp();
+            return;
+        }
+    }
     // the bitonic network needs a power of two: ceil(M / 32) registers per
     // lane, padded up to one (with kKeyMax)
     constexpr int R = (M + 31) / 32;
@@ -160,6 +181,7 @@ __device__ void compact_row(RowLists<M>& L, int r, int k, float nmax, int dp) {
     __syncwarp();
     if (lane == 0) {
         L.cnt[r] = min(uniq, k);
+        L.sorted[r] = min(uniq, k);
         if (m && kk < L.kth[r]) {
             L.kth[r] = kk;
             L.tau[r] = tau_from(kk, L.row_norm[r], nmax, dp);

@@ -272,6 +272,7 @@ struct TcSmem {
     float athr[kRT];                // approximate threshold of the row's list (+inf until k entries)
     float row_norm[kRT];
     int cnt[kRT];
+    int sorted[kRT];  // the row's list[0..sorted) is sorted (the last compaction's result)
     int mode[kRT];
     uint16_t queue[kEpiWarps][kTcQueue];  // exact-mode candidates (row << 8 | column) of the current tile
     float nb[kEpiWarps][2][kCT];          // column norms of the current and the next tile, per epilogue warp
@@ -336,6 +337,20 @@ static_assert(kListE == 4, "the compaction sorts 4 keys per lane");
 __noinline__ __device__ void compact_exact(TcSmem& sh, uint64_t* __restrict__ lst, int r, int k) {
     const int lane = threadIdx.x & 31;
     const int c = min(sh.cnt[r], kTcListRow);
+    {
+        const int s = sh.sorted[r];
+        if (s <= c && c - s <= 64) {  // merge the new entries into the sorted prefix
+            uint64_t kk;
+            const int kept = merge_sorted_prefix(lst, s, c, k, k - 1, [](uint64_t) { return kKeyMax; }, &kk);
+            if (lane == 0) {
+                sh.cnt[r] = kept;
+                sh.sorted[r] = kept;
+                if (kk != kKeyMax && kk < sh.kth[r]) sh.kth[r] = kk;
+            }
+            __syncwarp();
+            return;
+        }
+    }
     uint64_t v[kListE];
 #pragma unroll
     for (int j = 0; j < kListE; ++j) {
@@ -356,6 +371,7 @@ __noinline__ __device__ void compact_exact(TcSmem& sh, uint64_t* __restrict__ ls
     const uint64_t kk = __shfl_sync(0xffffffffu, kth_new, m ? __ffs(m) - 1 : 0);
     if (lane == 0) {
         sh.cnt[r] = min(uniq, k);
+        sh.sorted[r] = min(uniq, k);
         if (m && kk < sh.kth[r]) sh.kth[r] = kk;
     }
     __syncwarp();
@@ -369,6 +385,30 @@ __noinline__ __device__ int approx_compact(TcSmem& sh, uint64_t* __restrict__ ls
                                            float c4, int cap) {
     const int lane = threadIdx.x & 31;
     const int c = min(sh.cnt[r], kTcListRow);
+    {
+        const int s = sh.sorted[r];
+        if (s <= c && c - s <= 64) {  // merge the new entries into the sorted prefix
+            float thr = __int_as_float(0x7f800000);
+            uint64_t fk;
+            // entries above the margin over the k-th value are dropped (fewer
+            // than k entries: all are kept)
+            const int keep = merge_sorted_prefix(
+                lst, s, c, kTcListRow, k - 1,
+                [&](uint64_t key) -> uint64_t {
+                    if (key == kKeyMax) return kKeyMax;
+                    thr = approx_thr(unflip(key_bits(key)), c2, c3, c4);
+                    return (static_cast<uint64_t>(flip_bits(thr)) << 32) | 0xFFFFFFFFull;
+                },
+                &fk);
+            if (lane == 0) {
+                sh.cnt[r] = keep;
+                sh.sorted[r] = keep;
+                if (keep <= cap) sh.athr[r] = thr;
+            }
+            __syncwarp();
+            return keep;
+        }
+    }
     uint64_t v[kListE];
 #pragma unroll
     for (int j = 0; j < kListE; ++j) {
@@ -401,6 +441,7 @@ __noinline__ __device__ int approx_compact(TcSmem& sh, uint64_t* __restrict__ ls
         }
         if (lane == 0) {
             sh.cnt[r] = keep;
+            sh.sorted[r] = keep;
             sh.athr[r] = thr;
         }
     }
@@ -421,7 +462,10 @@ __noinline__ __device__ void to_exact_mode(TcSmem& sh, uint64_t* __restrict__ ls
         lst[e] = exact_key_lane(xr, ix, rbase + r, pb, d, dr);
     }
     __syncwarp();
-    if (lane == 0) sh.mode[r] = kModeExact;
+    if (lane == 0) {
+        sh.mode[r] = kModeExact;
+        sh.sorted[r] = 0;  // exact keys: the approximate order no longer holds
+    }
     __syncwarp();
     compact_exact(sh, lst, r, k);
 }
@@ -549,6 +593,7 @@ tc_sweep_kernel(const __grid_constant__ CUtensorMap tmap, const float* __restric
         sh.kth[r] = kth_shared[rbase + r];
         sh.row_norm[r] = cn[rbase + r];
         sh.cnt[r] = 0;
+        sh.sorted[r] = 0;
         sh.athr[r] = __int_as_float(0x7f800000);
         // with the filter disabled the f values carry no information: exact lists
         sh.mode[r] = scale->all != 0.0f ? kModeExact : kModeApprox;
@@ -764,7 +809,10 @@ tc_sweep_kernel(const __grid_constant__ CUtensorMap tmap, const float* __restric
                 const float c4 = __shfl_sync(0xffffffffu, rb.c4, i);
                 const int P = approx_compact(sh, lst, rr, k, c2, c3, c4, kTcListRow);
                 rescore_final(lst, rr, P, scratch, rbase, xr, ix, d, dr);
-                if (lane == 0) sh.mode[rr] = kModeExact;
+                if (lane == 0) {
+                    sh.mode[rr] = kModeExact;
+                    sh.sorted[rr] = 0;  // exact keys: the approximate order no longer holds
+                }
                 __syncwarp();
             }
             compact_exact(sh, lst, rr, k);

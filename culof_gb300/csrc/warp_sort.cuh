@@ -71,4 +71,86 @@ __device__ __forceinline__ int warp_unique_ranks(const uint64_t (&v)[E], uint64_
     return base;
 }
 
+// Number of entries of the ascending array a[0..len) below x (binary search).
+__device__ __forceinline__ int count_below(const uint64_t* a, int len, uint64_t x) {
+    int lo = 0, hi = len;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (a[mid] < x) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// Merge compaction of a list whose first s entries are sorted ascending and
+// whose entries s..c are new and unsorted (whole warp; keys unique; requires
+// s <= 128 and c - s <= 64). The new entries are sorted (a 64-key bitonic
+// network) and written back behind the prefix; every element's merged rank
+// is its index in its own run plus the number of smaller keys in the other
+// run (a binary search). Once the key of merged rank sel_rank is known
+// (kKeyMax if there is none), bound_fn(that key) gives an inclusive upper
+// bound: the merged keys <= bound, at most keep_max of them, are written to
+// lst[0..) in ascending order. Returns how many were kept; *sel receives the
+// selected key.
+template <typename BoundFn>
+__device__ __forceinline__ int merge_sorted_prefix(uint64_t* lst, int s, int c, int keep_max, int sel_rank,
+                                                   BoundFn bound_fn, uint64_t* sel) {
+    const int lane = threadIdx.x & 31;
+    const int u = c - s;
+    uint64_t v[2];
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+        const int e = j * 32 + lane;
+        v[j] = e < u ? lst[s + e] : ~0ull;
+    }
+    warp_bitonic_sort<2>(v);
+    __syncwarp();
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+        const int e = j * 32 + lane;
+        if (e < u) lst[s + e] = v[j];
+    }
+    __syncwarp();
+    uint64_t p[4];
+    int pr[4], vr[2];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const int e = j * 32 + lane;
+        p[j] = e < s ? lst[e] : ~0ull;
+        pr[j] = e < s ? e + count_below(lst + s, u, p[j]) : -1;
+    }
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+        const int e = j * 32 + lane;
+        vr[j] = e < u ? e + count_below(lst, s, v[j]) : -1;
+    }
+    uint64_t mine = ~0ull;
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+        if (pr[j] == sel_rank) mine = p[j];
+#pragma unroll
+    for (int j = 0; j < 2; ++j)
+        if (vr[j] == sel_rank) mine = v[j];
+    const unsigned m = __ballot_sync(0xffffffffu, mine != ~0ull);
+    const uint64_t picked = m ? __shfl_sync(0xffffffffu, mine, __ffs(m) - 1) : ~0ull;
+    *sel = picked;
+    const uint64_t bound = bound_fn(picked);
+    // merged keys <= bound form a prefix of the merged order
+    int below = 0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) below += __popc(__ballot_sync(0xffffffffu, pr[j] >= 0 && p[j] <= bound));
+#pragma unroll
+    for (int j = 0; j < 2; ++j) below += __popc(__ballot_sync(0xffffffffu, vr[j] >= 0 && v[j] <= bound));
+    const int keep = below < keep_max ? below : keep_max;
+    __syncwarp();
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+        if (pr[j] >= 0 && pr[j] < keep) lst[pr[j]] = p[j];
+#pragma unroll
+    for (int j = 0; j < 2; ++j)
+        if (vr[j] >= 0 && vr[j] < keep) lst[vr[j]] = v[j];
+    __syncwarp();
+    return keep;
+}
+
 }  // namespace culof_gb300

@@ -179,6 +179,7 @@ wide_sweep_kernel(const float* __restrict__ tiles, int nt, int nsplit, int d, in
                            ? __int_as_float(0xff800000)
                            : tau_from(kk, nr, nmax, dp_bound);
         H.L.cnt[tid] = 0;
+        H.L.sorted[tid] = 0;
     }
 
     auto issue = [&](int g) {
