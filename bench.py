@@ -88,6 +88,8 @@ def parse_args():
     p.add_argument("--path", choices=["auto", "fast", "general", "tensor"], default="auto")
     p.add_argument("--suite", action="store_true",
                    help="report harness: one JSON line per benchmark configuration (0-4) with an agreement gate")
+    p.add_argument("--scaling", action="store_true",
+                   help="the reference benchmark's n and d sweeps through culof_gb300.lof, gated bit-exact on the oracle")
     p.add_argument("--workload", choices=["clusters", "factor", "mixture"], default="clusters",
                    help="clusters: 5 clusters + 1%% outliers; factor: rank-16 factor model + 5.0 shift + 0.5%% noisy "
                         "rows; mixture: 8 clusters + 1%% outliers")
@@ -626,10 +628,56 @@ def run_suite(args):
     return 0
 
 
+def run_scaling(args):
+    """The reference benchmark's two sweeps (benchmarks/benchmark.py:187-205):
+    sample count n in {1k .. 200k} at d = 8, and dimensionality d in
+    {2, 8, 32, 128} at n = 20k, k = 20. Each row times the public host API
+    `culof_gb300.lof(X, k)` (fastest of 5 calls after one warm-up, wall clock,
+    host copies included, as benchmark.py:69-84 times `culof.lof`) and the
+    oracle on all host cores (one call), and gates on the scores: bit-exact
+    against the oracle, and the top-1% rank sets identical
+    (benchmark.py:101-116 allows 5% relative error against scikit-learn)."""
+    import torch
+
+    import culof_gb300
+    import oracle
+    from culof_gb300 import synthetic
+
+    torch.cuda.set_device(0)
+    culof_gb300.lof(synthetic.clusters_with_outliers(1000, 8, seed=0), 20)  # context init, excluded
+    rows = [("samples", n, 8) for n in (1_000, 2_000, 5_000, 10_000, 20_000, 50_000, 100_000, 200_000)]
+    rows += [("features", 20_000, d) for d in (2, 8, 32, 128)]
+    k = args.k
+    failed = False
+    for sweep, n, d in rows:
+        X = synthetic.clusters_with_outliers(n, d, seed=args.seed)
+        culof_gb300.lof(X, k)
+        best = float("inf")
+        for _ in range(5):
+            t0 = time.perf_counter()
+            s_gpu = culof_gb300.lof(X, k)
+            best = min(best, time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        s_cpu = oracle.lof(X, k)
+        t_cpu = time.perf_counter() - t0
+        rel = float(np.max(np.abs(s_gpu.astype(np.float64) - s_cpu) / np.maximum(np.abs(s_cpu), 1e-9)))
+        top = max(1, n // 100)
+        agree = len(set(np.argsort(-s_gpu, kind="stable")[:top]) & set(np.argsort(-s_cpu, kind="stable")[:top])) / top
+        exact = bool(np.array_equal(s_gpu.view(np.uint32), np.asarray(s_cpu, np.float32).view(np.uint32)))
+        failed |= not exact or agree < 1.0
+        print(json.dumps({"scaling": sweep, "n": n, "d": d, "k": k, "lof_s": best,
+                          "pair_dists_per_s": float(n) * n / best, "oracle_s": t_cpu,
+                          "oracle_threads": os.cpu_count(), "speedup_vs_oracle": t_cpu / best,
+                          "max_rel_err": rel, "rank_agreement": agree, "bit_exact_vs_oracle": exact}), flush=True)
+    return 1 if failed else 0
+
+
 def main():
     args = parse_args()
     if args.suite:
         return run_suite(args)
+    if args.scaling:
+        return run_scaling(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)
