@@ -48,6 +48,7 @@ using namespace sweep;
 constexpr int kPairs = kCT / 2;
 constexpr int kRowsPerLane = 4;
 constexpr int kStages = 4;     // column tiles in flight
+constexpr int kSeedWindow = 3;  // tiles of the seed: T, T+1, T-1
 constexpr int kMaxDP = 8;      // the small-d sweep; wider points take wide.cu's
 constexpr int kMaxWideD = 128;
 constexpr int kMortonDims = 8;  // Morton key over (up to) the 8 widest dimensions
@@ -315,9 +316,13 @@ __device__ __forceinline__ float tile_dist2(const float* ta, int ca, const float
     return s;
 }
 
-// Per row of tile T: the exact k best keys over tile T's own columns (sorted,
+// Per row of tile T: the exact k best keys over the seed window (sorted,
 // kKeyMax padded) and its k-th key, the starting point of the row's shared
-// k-th key (kth_shared) that the sweep CTAs tighten with atomicMin.
+// k-th key (kth_shared) that the sweep CTAs tighten with atomicMin. The
+// window is the first qs spiral positions: tile T itself and its Morton
+// neighbours T+1 and T-1, whose points start the k-th distances much closer
+// to their final values than tile T alone (fewer candidates reach the
+// sweep's lists); the sweep covers the spiral from position qs on.
 // Pruning margin: the float32 direct-difference distance D of two points at
 // real squared distance T >= LB satisfies D >= T (1 - (d + 2) 2^-24) >
 // LB (1 - 2^-20) for d <= 8, so a tile whose rounded-down box gap times
@@ -391,7 +396,7 @@ __global__ void order_key_kernel(const int* __restrict__ pcount, int nt, unsigne
 // order, each with its rounded-down box gap (the sweep re-tests the gap
 // against its tighter current k-th distances without touching the boxes).
 template <int DP>
-__global__ void __launch_bounds__(256) prune_list_kernel(const float* __restrict__ boxes, int nt,
+__global__ void __launch_bounds__(256) prune_list_kernel(const float* __restrict__ boxes, int nt, int qs,
                                                          const unsigned long long* __restrict__ kth_seed,
                                                          uint2* __restrict__ plist, int* __restrict__ pcount) {
     __shared__ float tbox[2][DP];
@@ -417,7 +422,7 @@ __global__ void __launch_bounds__(256) prune_list_kernel(const float* __restrict
     __syncthreads();
     const float kmax = kmax_s;
     uint2* out = plist + static_cast<int64_t>(T) * nt;
-    for (int q0 = 1; q0 < nt; q0 += 256) {
+    for (int q0 = qs; q0 < nt; q0 += 256) {
         const int q = q0 + static_cast<int>(threadIdx.x);
         bool pass = false;
         unsigned t = 0;
@@ -451,39 +456,88 @@ __global__ void __launch_bounds__(256) prune_list_kernel(const float* __restrict
 
 template <int DP>
 __global__ void __launch_bounds__(kThreads) seed_kernel(const float* __restrict__ tiles, int nt, int64_t n, int k,
-                                                        uint64_t* __restrict__ seed_keys,
+                                                        int qs, uint64_t* __restrict__ seed_keys,
                                                         unsigned long long* __restrict__ kth_shared) {
-    __shared__ __align__(16) float tile[tile_floats(DP)];
+    __shared__ __align__(16) float tile[kSeedWindow][tile_floats(DP)];
+    __shared__ uint64_t wl[kWarps][96];  // per warp: the row's sorted k best (k <= 64), then up to 32 new keys
     const int T = blockIdx.x;
-    const float* src = tiles + static_cast<int64_t>(T) * tile_floats(DP);
-    for (int i = threadIdx.x; i < tile_floats(DP); i += kThreads) tile[i] = src[i];
+    for (int q = 0; q < qs; ++q) {
+        const float* src = tiles + static_cast<int64_t>(spiral_tile(T, q, nt)) * tile_floats(DP);
+        for (int i = threadIdx.x; i < tile_floats(DP); i += kThreads) tile[q][i] = src[i];
+    }
     __syncthreads();
-    const unsigned* idx = reinterpret_cast<const unsigned*>(tile + tile_index_off(DP));
+    const unsigned* idx = reinterpret_cast<const unsigned*>(tile[0] + tile_index_off(DP));
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint64_t* lst = wl[warp];
+    const auto exact = [](uint64_t key) { return key; };
     for (int r = warp; r < kRT; r += kWarps) {
         const int64_t pos = static_cast<int64_t>(T) * kRT + r;
         const bool row_valid = idx[r] != kNoIndex;
+        // own tile: sort all 128 keys
         uint64_t v[4];
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             const int c = j * 32 + lane;
             uint64_t key = kKeyMax;
             if (row_valid && c != r && idx[c] != kNoIndex)
-                key = make_key(__float_as_uint(tile_dist2<DP>(tile, r, tile, c)), idx[c]);
+                key = make_key(__float_as_uint(tile_dist2<DP>(tile[0], r, tile[0], c)), idx[c]);
             v[j] = key;
         }
         warp_bitonic_sort<4>(v);
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const int e = j * 32 + lane;
-            if (e < k) seed_keys[pos * k + e] = v[j];
-        }
         const int owner = (k - 1) & 31, oreg = (k - 1) >> 5;
         uint64_t kk = kKeyMax;
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             const uint64_t t = __shfl_sync(0xffffffffu, v[j], owner);
             if (j == oreg) kk = t;
+        }
+        if (row_valid && qs > 1) {
+            // neighbour tiles: append the keys below the current k-th key and
+            // merge them into the sorted k best (at most 32 at a time)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int e = j * 32 + lane;
+                if (e < k) lst[e] = v[j];
+            }
+            float ra[DP];
+#pragma unroll
+            for (int f = 0; f < DP; ++f) ra[f] = tile_coord<DP>(tile[0], r, f);
+            int cnt = k;
+            for (int q = 1; q < qs; ++q) {
+                const unsigned* idq = reinterpret_cast<const unsigned*>(tile[q] + tile_index_off(DP));
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const int c = j * 32 + lane;
+                    float d2 = 0.0f;  // tile_dist2's arithmetic, row coordinates in registers
+#pragma unroll
+                    for (int f = 0; f < DP; ++f) {
+                        const float t = __fsub_rn(ra[f], tile_coord<DP>(tile[q], c, f));
+                        d2 = __fmaf_rn(t, t, d2);
+                    }
+                    const uint64_t key = idq[c] != kNoIndex ? make_key(__float_as_uint(d2), idq[c]) : kKeyMax;
+                    unsigned m = __ballot_sync(0xffffffffu, key < kk);
+                    if (m && cnt + __popc(m) > k + 32) {
+                        __syncwarp();
+                        cnt = merge_sorted_prefix<1>(lst, k, cnt, k, k - 1, exact, &kk);
+                        m = __ballot_sync(0xffffffffu, key < kk);
+                    }
+                    if (m) {
+                        __syncwarp();
+                        if (key < kk) lst[cnt + __popc(m & ((1u << lane) - 1u))] = key;
+                        cnt += __popc(m);
+                    }
+                }
+            }
+            __syncwarp();
+            if (cnt > k) cnt = merge_sorted_prefix<1>(lst, k, cnt, k, k - 1, exact, &kk);
+            for (int e = lane; e < k; e += 32) seed_keys[pos * k + e] = lst[e];
+            __syncwarp();
+        } else {
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int e = j * 32 + lane;
+                if (e < k) seed_keys[pos * k + e] = v[j];
+            }
         }
         if (lane == 0) kth_shared[pos] = row_valid ? kk : kKeyMax;
     }
@@ -548,7 +602,8 @@ __device__ bool drain_queue(SweepSmem<DP, M>& sh, int qc, const float* __restric
 // arrive by TMA and the last warp to finish a tile refills its stage.
 template <int DP, int M>
 __global__ void __launch_bounds__(kThreads, 2)
-sweep_kernel(const float* __restrict__ tiles, int nt, int nsplit, int k, const unsigned* __restrict__ max_norm_bits,
+sweep_kernel(const float* __restrict__ tiles, int nt, int qs, int nsplit, int k,
+             const unsigned* __restrict__ max_norm_bits,
              unsigned long long* __restrict__ kth_shared, uint64_t* __restrict__ partial, int* __restrict__ status,
              unsigned long long* __restrict__ evaluated_blocks, const uint2* __restrict__ plist,
              const int* __restrict__ pcount, const unsigned* __restrict__ order) {
@@ -566,8 +621,9 @@ sweep_kernel(const float* __restrict__ tiles, int nt, int nsplit, int k, const u
     // this split's share of the row tile's candidate column tiles: entries
     // split + nsplit j of its list (visiting order, interleaved, so every
     // split meets the nearby tiles first)
-    // (without lists, very large n: every other tile in spiral order)
-    const int lcount = plist ? pcount[T] : nt - 1;
+    // (without lists, very large n: every tile past the seed window in
+    // spiral order)
+    const int lcount = plist ? pcount[T] : nt - qs;
     const int count = lcount > split ? (lcount - split + nsplit - 1) / nsplit : 0;
     const uint2* tlist = plist ? plist + static_cast<int64_t>(T) * nt : nullptr;
     constexpr unsigned kTileBytes = tile_bytes(DP);
@@ -669,7 +725,7 @@ sweep_kernel(const float* __restrict__ tiles, int nt, int nsplit, int k, const u
                     t = static_cast<int>(e.x);
                     pass = !(__fmul_rd(__uint_as_float(e.y), kPruneShrink) > kmax);
                 } else {
-                    t = spiral_tile(T, 1 + split + nsplit * j, nt);
+                    t = spiral_tile(T, qs + split + nsplit * j, nt);
                     pass = true;
                 }
             }
@@ -929,13 +985,14 @@ int choose_splits(int nt, int sms) {
 namespace {
 
 template <int DP, int M>
-void launch_sweep(const float* tiles, int nt, int nsplit, int k, const unsigned* maxn, unsigned long long* kth_shared,
+void launch_sweep(const float* tiles, int nt, int qs, int nsplit, int k, const unsigned* maxn,
+                  unsigned long long* kth_shared,
                   uint64_t* partial, int* status, unsigned long long* evaluated, const uint2* plist, const int* pcount,
                   const unsigned* order, cudaStream_t s) {
     const size_t smem = sizeof(SweepSmem<DP, M>);
     set_max_dynamic_smem(reinterpret_cast<const void*>(sweep_kernel<DP, M>), static_cast<int>(smem));
-    sweep_kernel<DP, M><<<nt * nsplit, kThreads, smem, s>>>(tiles, nt, nsplit, k, maxn, kth_shared, partial, status,
-                                                            evaluated, plist, pcount, order);
+    sweep_kernel<DP, M><<<nt * nsplit, kThreads, smem, s>>>(tiles, nt, qs, nsplit, k, maxn, kth_shared, partial,
+                                                            status, evaluated, plist, pcount, order);
     CG_LAUNCH_CHECK();
 }
 
@@ -1014,6 +1071,10 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
         const long v = std::atol(env);
         if (v >= 1 && nt > 1) nsplit = static_cast<int>(v < nt - 1 ? v : nt - 1);
     }
+    // the small-d seed covers the first qs spiral positions of every row
+    // tile, the sweep the rest (the wide and tensor seeds cover tile T alone)
+    const int qs = (wide || tensor) ? 1 : (nt < kSeedWindow ? nt : kSeedWindow);
+    const bool sweep = nt > qs;
 
     // 1. Morton keys of the centred coordinates, then a stable radix sort.
     unsigned* mm = reinterpret_cast<unsigned*>(sort_hist_.get(2 * sizeof(unsigned) * d + sizeof(int) * kMortonDims));
@@ -1094,10 +1155,10 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
     if (tensor) tc_seed(tcb, nt, d, k, seed_keys, kth_shared, s);
     else if (wide) wide_seed(tiles, nt, d, k, seed_keys, kth_shared, s);
     else switch (dp) {
-        case 2: seed_kernel<2><<<nt, kThreads, 0, s>>>(tiles, nt, n, k, seed_keys, kth_shared); break;
-        case 4: seed_kernel<4><<<nt, kThreads, 0, s>>>(tiles, nt, n, k, seed_keys, kth_shared); break;
-        case 6: seed_kernel<6><<<nt, kThreads, 0, s>>>(tiles, nt, n, k, seed_keys, kth_shared); break;
-        default: seed_kernel<8><<<nt, kThreads, 0, s>>>(tiles, nt, n, k, seed_keys, kth_shared); break;
+        case 2: seed_kernel<2><<<nt, kThreads, 0, s>>>(tiles, nt, n, k, qs, seed_keys, kth_shared); break;
+        case 4: seed_kernel<4><<<nt, kThreads, 0, s>>>(tiles, nt, n, k, qs, seed_keys, kth_shared); break;
+        case 6: seed_kernel<6><<<nt, kThreads, 0, s>>>(tiles, nt, n, k, qs, seed_keys, kth_shared); break;
+        default: seed_kernel<8><<<nt, kThreads, 0, s>>>(tiles, nt, n, k, qs, seed_keys, kth_shared); break;
     }
     if (!wide && !tensor) CG_LAUNCH_CHECK();
     mark(3);
@@ -1107,14 +1168,14 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
     int* pcount = nullptr;
     const unsigned* order = nullptr;
     constexpr int kMaxListTiles = 16384;  // lists take nt^2 x 8 bytes: up to 2 GiB
-    if (!wide && !tensor && nt > 1 && nt <= kMaxListTiles) {
+    if (!wide && !tensor && sweep && nt <= kMaxListTiles) {
         plist = plist_.as<uint2>(static_cast<size_t>(nt) * nt);
         pcount = pcount_.as<int>(nt);
         switch (dp) {
-            case 2: prune_list_kernel<2><<<nt, 256, 0, s>>>(boxes, nt, kth_shared, plist, pcount); break;
-            case 4: prune_list_kernel<4><<<nt, 256, 0, s>>>(boxes, nt, kth_shared, plist, pcount); break;
-            case 6: prune_list_kernel<6><<<nt, 256, 0, s>>>(boxes, nt, kth_shared, plist, pcount); break;
-            default: prune_list_kernel<8><<<nt, 256, 0, s>>>(boxes, nt, kth_shared, plist, pcount); break;
+            case 2: prune_list_kernel<2><<<nt, 256, 0, s>>>(boxes, nt, qs, kth_shared, plist, pcount); break;
+            case 4: prune_list_kernel<4><<<nt, 256, 0, s>>>(boxes, nt, qs, kth_shared, plist, pcount); break;
+            case 6: prune_list_kernel<6><<<nt, 256, 0, s>>>(boxes, nt, qs, kth_shared, plist, pcount); break;
+            default: prune_list_kernel<8><<<nt, 256, 0, s>>>(boxes, nt, qs, kth_shared, plist, pcount); break;
         }
         CG_LAUNCH_CHECK();
     }
@@ -1134,17 +1195,18 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
     unsigned long long* evaluated = reinterpret_cast<unsigned long long*>(pair_stats_.get(2 * sizeof(unsigned long long)));
     CG_CUDA(cudaMemsetAsync(evaluated, 0, 2 * sizeof(unsigned long long), s));
     stat_total_blocks_ = (!wide && !tensor && nt > 1) ? static_cast<unsigned long long>(nt) * (nt - 1) * kWarps : 0;
+    stat_seed_blocks_ = (!wide && !tensor) ? static_cast<unsigned long long>(nt) * (qs - 1) * kWarps : 0;
     if (nt > 1 && tensor) {
         uint64_t* lists = static_cast<uint64_t*>(tc_lists_.get(tc_list_bytes(nt, nsplit)));
         tc_sweep(tcb, nt, nsplit, d, k, maxn, kth_shared, partial, lists, status, s);
     } else if (nt > 1 && wide) {
         wide_sweep(tiles, nt, nsplit, d, k, maxn, kth_shared, partial, s);
-    } else if (nt > 1) {
+    } else if (sweep) {
         const bool big = k > 32;
 #define CG_SWEEP(DPV)                                                                                 \
-    (big ? launch_sweep<DPV, 96>(tiles, nt, nsplit, k, maxn, kth_shared, partial, status, evaluated, plist, pcount, \
+    (big ? launch_sweep<DPV, 96>(tiles, nt, qs, nsplit, k, maxn, kth_shared, partial, status, evaluated, plist, pcount, \
                                  order, s)                                                                         \
-         : launch_sweep<DPV, 64>(tiles, nt, nsplit, k, maxn, kth_shared, partial, status, evaluated, plist, pcount, \
+         : launch_sweep<DPV, 64>(tiles, nt, qs, nsplit, k, maxn, kth_shared, partial, status, evaluated, plist, pcount, \
                                  order, s))
         switch (dp) {
             case 2: CG_SWEEP(2); break;
@@ -1154,7 +1216,7 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
         }
 #undef CG_SWEEP
     }
-    const int ns = nt > 1 ? nsplit : 0;
+    const int ns = sweep ? nsplit : 0;
     mark(4);
 
     // 5. merge into the reference slot order

@@ -84,7 +84,7 @@ __device__ __forceinline__ int count_below(const uint64_t* a, int len, uint64_t 
 
 // Merge compaction of a list whose first s entries are sorted ascending and
 // whose entries s..c are new and unsorted (whole warp; keys unique; requires
-// s <= 128 and c - s <= 64). The new entries are sorted (a 64-key bitonic
+// s <= 128 and c - s <= 32 E). The new entries are sorted (a 32 E-key bitonic
 // network) and written back behind the prefix; every element's merged rank
 // is its index in its own run plus the number of smaller keys in the other
 // run (a binary search). Once the key of merged rank sel_rank is known
@@ -92,27 +92,27 @@ __device__ __forceinline__ int count_below(const uint64_t* a, int len, uint64_t 
 // bound: the merged keys <= bound, at most keep_max of them, are written to
 // lst[0..) in ascending order. Returns how many were kept; *sel receives the
 // selected key.
-template <typename BoundFn>
+template <int E = 2, typename BoundFn>
 __device__ __forceinline__ int merge_sorted_prefix(uint64_t* lst, int s, int c, int keep_max, int sel_rank,
                                                    BoundFn bound_fn, uint64_t* sel) {
     const int lane = threadIdx.x & 31;
     const int u = c - s;
-    uint64_t v[2];
+    uint64_t v[E];
 #pragma unroll
-    for (int j = 0; j < 2; ++j) {
+    for (int j = 0; j < E; ++j) {
         const int e = j * 32 + lane;
         v[j] = e < u ? lst[s + e] : ~0ull;
     }
-    warp_bitonic_sort<2>(v);
+    warp_bitonic_sort<E>(v);
     __syncwarp();
 #pragma unroll
-    for (int j = 0; j < 2; ++j) {
+    for (int j = 0; j < E; ++j) {
         const int e = j * 32 + lane;
         if (e < u) lst[s + e] = v[j];
     }
     __syncwarp();
     uint64_t p[4];
-    int pr[4], vr[2];
+    int pr[4], vr[E];
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
         const int e = j * 32 + lane;
@@ -120,7 +120,7 @@ __device__ __forceinline__ int merge_sorted_prefix(uint64_t* lst, int s, int c, 
         pr[j] = e < s ? e + count_below(lst + s, u, p[j]) : -1;
     }
 #pragma unroll
-    for (int j = 0; j < 2; ++j) {
+    for (int j = 0; j < E; ++j) {
         const int e = j * 32 + lane;
         vr[j] = e < u ? e + count_below(lst, s, v[j]) : -1;
     }
@@ -129,7 +129,7 @@ __device__ __forceinline__ int merge_sorted_prefix(uint64_t* lst, int s, int c, 
     for (int j = 0; j < 4; ++j)
         if (pr[j] == sel_rank) mine = p[j];
 #pragma unroll
-    for (int j = 0; j < 2; ++j)
+    for (int j = 0; j < E; ++j)
         if (vr[j] == sel_rank) mine = v[j];
     const unsigned m = __ballot_sync(0xffffffffu, mine != ~0ull);
     const uint64_t picked = m ? __shfl_sync(0xffffffffu, mine, __ffs(m) - 1) : ~0ull;
@@ -140,14 +140,14 @@ __device__ __forceinline__ int merge_sorted_prefix(uint64_t* lst, int s, int c, 
 #pragma unroll
     for (int j = 0; j < 4; ++j) below += __popc(__ballot_sync(0xffffffffu, pr[j] >= 0 && p[j] <= bound));
 #pragma unroll
-    for (int j = 0; j < 2; ++j) below += __popc(__ballot_sync(0xffffffffu, vr[j] >= 0 && v[j] <= bound));
+    for (int j = 0; j < E; ++j) below += __popc(__ballot_sync(0xffffffffu, vr[j] >= 0 && v[j] <= bound));
     const int keep = below < keep_max ? below : keep_max;
     __syncwarp();
 #pragma unroll
     for (int j = 0; j < 4; ++j)
         if (pr[j] >= 0 && pr[j] < keep) lst[pr[j]] = p[j];
 #pragma unroll
-    for (int j = 0; j < 2; ++j)
+    for (int j = 0; j < E; ++j)
         if (vr[j] >= 0 && vr[j] < keep) lst[vr[j]] = v[j];
     __syncwarp();
     return keep;

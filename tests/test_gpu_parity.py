@@ -75,6 +75,10 @@ KNN_CASES = [
     ("k64", lambda: synthetic.clusters_with_outliers(5000, 8, seed=23), 64),
     ("k33_d3", lambda: synthetic.clusters_with_outliers(3000, 3, seed=24), 33),
     ("d1", lambda: synthetic.clusters_with_outliers(2000, 1, seed=25), 10),
+    # the small-d seed covers tiles T, T+1, T-1: three tiles leave the sweep
+    # nothing; four leave it one tile per row tile
+    ("n300_seed_only", lambda: synthetic.clusters_with_outliers(300, 8, seed=29), 20),
+    ("n385_k64", lambda: synthetic.clusters_with_outliers(385, 6, seed=30), 64),
     # the wide-point sweep: d not a multiple of 16, d = 128 with k = 50
     ("d9", lambda: synthetic.clusters_with_outliers(3000, 9, seed=26), 20),
     ("d100_k40", lambda: synthetic.reference_test_data(2500, 100, seed=27, n_outliers=25), 40),
