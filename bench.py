@@ -13,8 +13,10 @@ offset and the labels.
   buffers: host->device copy of X, the pipeline and the device->host copy of
   nof + labels + offset, every step (wall time of the synchronous call).
 * roofline: the distance sweep kernel (the dominant kernel): the algorithmic
-  work, 2d FLOP for each of the n (n - 128) pairs outside the rows' own tiles
-  (one evaluation per pair), over its event time, against the measured FP32
+  work, 2d FLOP for each of the n (n - 384) pairs outside the rows' seed
+  windows (the own tile and its two Morton neighbour tiles, which the seed
+  kernel covers; one evaluation per pair), over its event time, against the
+  measured FP32
   FMA peak. The kernel skips column tiles that a bounding-box test proves
   farther than every k-th neighbour; the pairs it actually evaluated, the
   pruned fraction and its FLOP rate on the evaluated pairs are reported
@@ -57,8 +59,8 @@ PATH_NAMES = ["auto", "fast", "general", "tensor"]
 # very workload (dram__bytes_read.sum + dram__bytes_write.sum); other
 # workloads report null.
 MEASURED_SWEEP_TRAFFIC = {
-    ("clusters", 200_000, 8, 20): (18_867_712 + 76_127_488,
-                                   "ncu: 18.9 MB read + 76.1 MB written per sweep_kernel launch at this workload"),
+    ("clusters", 200_000, 8, 20): (17_980_000 + 74_240_000,
+                                   "ncu: 17.98 MB read + 74.24 MB written per sweep_kernel launch at this workload"),
 }
 
 
@@ -389,9 +391,12 @@ def run_ours(args):
 
     stages = {name: statistics.mean(v) for name, v in stage_acc.items()}
     fp32_peak = max(_culof.probe_fp32_tflops(True), _culof.probe_fp32_tflops(False))
-    # the sweep evaluates every pair outside the row's own 128-point tile
+    # the sweep evaluates every pair outside the rows' seed window: the own
+    # 128-point tile (tensor and wide paths), or the own tile and its two
+    # Morton neighbour tiles (small-d path, d <= 8)
     nt = (n + 127) // 128
-    sweep_pairs = float(n) * float(n - min(n, 128)) if nt > 1 else 0.0
+    window = min(nt, 3) if (ctx.last_path() == _culof.PATH_FAST and d <= 8) else 1
+    sweep_pairs = float(n) * float(n - min(n, 128 * window)) if nt > window else 0.0
     sweep_ms = stages.get("sweep")
     roofline = None
     if sweep_ms and sweep_pairs > 0 and ctx.last_path() == _culof.PATH_TENSOR:
@@ -413,7 +418,7 @@ def run_ours(args):
             "sweep_share_of_step": sweep_ms / mean_ms,
         }
     elif sweep_ms and sweep_pairs > 0 and ctx.last_path() == _culof.PATH_FAST:
-        # algorithmic work: 2d FLOP for every pair outside the row's own tile
+        # algorithmic work: 2d FLOP for every pair past the row's seed window
         # (one evaluation per pair); the kernel itself evaluates only the
         # pairs of column tiles a bounding-box test cannot rule out, and its
         # efficiency on those is reported beside it

@@ -159,7 +159,6 @@ void Engine::knn(const float* d_x, int64_t n, int d, int k, bool normalize, int3
     unsigned int* maxn = max_norm_.as<unsigned int>(1);
     CG_CUDA(cudaMemsetAsync(status_ptr(), 0, sizeof(int), stream_));
     stat_total_blocks_ = 0;
-    stat_seed_blocks_ = 0;
     for (bool& m : marked_) m = false;
     mark(0);
     center(d_x, n, d, normalize, xc, partial, mean, inv, stream_);
@@ -261,7 +260,7 @@ void Engine::pair_stats(double* evaluated, double* total) {
         CG_CUDA(cudaStreamSynchronize(stream_));
     }
     // one block = 16 rows x 128 columns
-    if (evaluated) *evaluated = static_cast<double>(ev + stat_seed_blocks_) * 16.0 * 128.0;
+    if (evaluated) *evaluated = static_cast<double>(ev) * 16.0 * 128.0;
     if (total) *total = static_cast<double>(stat_total_blocks_) * 16.0 * 128.0;
 }
 

@@ -158,7 +158,6 @@ private:
     // would evaluate without pruning
     DevBuf pair_stats_, boxes_, plist_, pcount_, order_;
     unsigned long long stat_total_blocks_ = 0;
-    unsigned long long stat_seed_blocks_ = 0;  // blocks the small-d seed evaluates beyond tile T
     // Device status word of the current call: kernels set it (a bounded wait
     // that expired, an out-of-range neighbour index); host paths check it.
     DevBuf status_;

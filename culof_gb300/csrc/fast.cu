@@ -1194,8 +1194,8 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
     // 4. sweep over the other tiles, split S ways
     unsigned long long* evaluated = reinterpret_cast<unsigned long long*>(pair_stats_.get(2 * sizeof(unsigned long long)));
     CG_CUDA(cudaMemsetAsync(evaluated, 0, 2 * sizeof(unsigned long long), s));
-    stat_total_blocks_ = (!wide && !tensor && nt > 1) ? static_cast<unsigned long long>(nt) * (nt - 1) * kWarps : 0;
-    stat_seed_blocks_ = (!wide && !tensor) ? static_cast<unsigned long long>(nt) * (qs - 1) * kWarps : 0;
+    // every (warp, column tile) block past the seed window
+    stat_total_blocks_ = (!wide && !tensor && sweep) ? static_cast<unsigned long long>(nt) * (nt - qs) * kWarps : 0;
     if (nt > 1 && tensor) {
         uint64_t* lists = static_cast<uint64_t*>(tc_lists_.get(tc_list_bytes(nt, nsplit)));
         tc_sweep(tcb, nt, nsplit, d, k, maxn, kth_shared, partial, lists, status, s);

@@ -114,8 +114,9 @@ CULOF_API int culof_context_stage_times(culof_context* ctx, float* ms, int cap);
 CULOF_API unsigned long long culof_kernel_launch_count(void);
 /* Row x column pairs the last small-d FP32 sweep of this context evaluated
  * (tiles that a bounding-box test proves farther than every k-th neighbour
- * are skipped) and the pairs it would evaluate without that test; both 0
- * after other paths. Synchronises the context stream. */
+ * are skipped) and the pairs it would evaluate without that test (every
+ * column tile past the seed's own and two neighbour tiles); both 0 after
+ * other paths. Synchronises the context stream. */
 CULOF_API int culof_context_pair_stats(culof_context* ctx, double* evaluated_pairs, double* total_pairs);
 
 /* Measured FP32 CUDA-core throughput of the current device in TFLOP/s
