@@ -231,6 +231,21 @@ def test_lrd_and_score_stage_entry_points():
     np.testing.assert_array_equal(host(sc), oracle.score(idx, o_lrd))
 
 
+@pytest.mark.parametrize("n,swept", [(20_000, True), (300, False)])
+def test_pair_stats_cover_the_sweep_past_the_seed_window(ctx, n, swept):
+    # the small-d seed covers tiles T, T+1, T-1; the sweep every later tile
+    X = synthetic.clusters_with_outliers(n, 8, seed=31)
+    ctx.set_path(_culof.PATH_FAST)
+    ctx.lof(X, 20)
+    ev, tot = ctx.pair_stats()
+    nt = (n + 127) // 128
+    if swept:
+        assert tot == nt * (nt - 3) * 128 * 128
+        assert 0 < ev <= tot
+    else:
+        assert ev == 0 and tot == 0
+
+
 def test_repeated_calls_are_bit_identical(ctx):
     X = synthetic.reference_test_data(512, 6, seed=17, n_outliers=7)
     first = ctx.lof(X, 20)
