@@ -769,6 +769,7 @@ sweep_kernel(const float* __restrict__ tiles, int nt, int qs, int nsplit, int k,
         for (int st = 0; st < kStages; ++st) fill(st, st);
 
     bool ok = true;
+    unsigned evaluated = 0;  // this warp's evaluated (not pruned) column tiles
     for (int m = 0; ok; ++m) {
         const int stage = m % kStages;
         if (!mbar_wait_warp(&sh.full_bar[stage], (m / kStages) & 1)) {
@@ -782,7 +783,7 @@ sweep_kernel(const float* __restrict__ tiles, int nt, int qs, int nsplit, int k,
         // prune: the whole tile is farther than every row's k-th distance
         const float* tb = tl + tile_box_off(DP);
         const bool skip = __fmul_rd(box_gap2_rd<DP>(sh.wbox[warp][0], sh.wbox[warp][1], tb, tb + DP), kPruneShrink) > wk;
-        if (!skip && lane == 0) atomicAdd(&sh.evaluated, 1u);
+        evaluated += skip ? 0u : 1u;
 #pragma unroll 2
         for (int s = 0; s < (skip ? 0 : kPairs / 8); ++s) {
             const int p = s * 8 + cp;
@@ -874,6 +875,7 @@ sweep_kernel(const float* __restrict__ tiles, int nt, int qs, int nsplit, int k,
             fill(stage, m + kStages);
         }
     }
+    if (lane == 0) atomicAdd(&sh.evaluated, evaluated);
     const int failed = __syncthreads_or(ok ? 0 : 1);
     if (tid == 0 && evaluated_blocks) atomicAdd(evaluated_blocks, static_cast<unsigned long long>(sh.evaluated));
     if (failed) {
