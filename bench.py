@@ -90,6 +90,8 @@ def parse_args():
     p.add_argument("--path", choices=["auto", "fast", "general", "tensor"], default="auto")
     p.add_argument("--suite", action="store_true",
                    help="report harness: one JSON line per benchmark configuration (0-4) with an agreement gate")
+    p.add_argument("--batched", type=int, default=0, metavar="N",
+                   help="config 4's batched workload alone with N problems (batched call against single calls)")
     p.add_argument("--scaling", action="store_true",
                    help="the reference benchmark's n and d sweeps through culof_gb300.lof, gated bit-exact on the oracle")
     p.add_argument("--workload", choices=["clusters", "factor", "mixture"], default="clusters",
@@ -510,6 +512,44 @@ def _time_calls(fn, stream, warm=2, reps=5):
     return e0.elapsed_time(e1) / reps
 
 
+def batched_case(count, stream, emit, label):
+    """Config 4's workload with `count` problems: one batched call (CUDA
+    graph replay after the first call) against a loop of single calls, and
+    the scores of both compared bit for bit."""
+    import torch
+
+    from culof_gb300 import _culof, synthetic
+
+    probs, ks = synthetic.batched_problems(count, 16, seed=0)
+    Xb = np.concatenate(probs).astype(np.float32)
+    offs = np.zeros(len(probs) + 1, np.int64)
+    offs[1:] = np.cumsum([len(p) for p in probs])
+    ctx = _culof.Context()
+    ctx.set_stream(stream.cuda_stream)
+    dX = torch.from_numpy(Xb).cuda()
+    ds = torch.empty(len(Xb), device="cuda")
+    t0 = time.perf_counter()
+    ctx.lof_batched_device(offs, ks, dX.data_ptr(), 16, False, ds.data_ptr())
+    ctx.synchronize()
+    first_s = time.perf_counter() - t0
+    ms_b = _time_calls(lambda: ctx.lof_batched_device(offs, ks, dX.data_ptr(), 16, False, ds.data_ptr()), stream)
+    dps = [dX[offs[i]:offs[i + 1]] for i in range(len(probs))]
+    outs = torch.empty_like(ds)
+
+    def loop():
+        for i in range(len(probs)):
+            ctx.lof_device(dps[i].data_ptr(), len(probs[i]), 16, ks[i], False, outs[offs[i]:offs[i + 1]].data_ptr())
+
+    ms_l = _time_calls(loop, stream, warm=1, reps=2)
+    same = bool(np.array_equal(ds.cpu().numpy().view(np.uint32), outs.cpu().numpy().view(np.uint32)))
+    emit({"suite": label, "problems": len(probs), "points": int(offs[-1]), "d": 16,
+          "pairs": float(sum(float(len(p)) ** 2 for p in probs)),
+          "batched_s": ms_b * 1e-3, "loop_of_single_calls_s": ms_l * 1e-3, "speedup_vs_loop": ms_l / ms_b,
+          "first_call_s_plan_autotune_capture": first_s,
+          "agreement": {"bit_exact_vs_single_calls": same}})
+    ctx.close()
+
+
 def run_suite(args):
     """One JSON line per benchmark configuration, each with its timing and an
     agreement gate against the oracle or an independent exact path (the
@@ -602,34 +642,7 @@ def run_suite(args):
           "backward_s": (ms_fb - ms_f) * 1e-3, "forward_backward_s": ms_fb * 1e-3,
           "agreement": {"grad_max_rel_err_vs_fp64_autograd": rel, "float32_result": True}})
     # config 4: 2,048 problems in one batched call against a loop of single calls
-    probs, ks = synthetic.batched_problems(2048, 16, seed=0)
-    Xb = np.concatenate(probs).astype(np.float32)
-    offs = np.zeros(len(probs) + 1, np.int64)
-    offs[1:] = np.cumsum([len(p) for p in probs])
-    ctx = _culof.Context()
-    ctx.set_stream(stream.cuda_stream)
-    dX = torch.from_numpy(Xb).cuda()
-    ds = torch.empty(len(Xb), device="cuda")
-    t0 = time.perf_counter()
-    ctx.lof_batched_device(offs, ks, dX.data_ptr(), 16, False, ds.data_ptr())
-    ctx.synchronize()
-    first_s = time.perf_counter() - t0
-    ms_b = _time_calls(lambda: ctx.lof_batched_device(offs, ks, dX.data_ptr(), 16, False, ds.data_ptr()), stream)
-    dps = [dX[offs[i]:offs[i + 1]] for i in range(len(probs))]
-    outs = torch.empty_like(ds)
-
-    def loop():
-        for i in range(len(probs)):
-            ctx.lof_device(dps[i].data_ptr(), len(probs[i]), 16, ks[i], False, outs[offs[i]:offs[i + 1]].data_ptr())
-
-    ms_l = _time_calls(loop, stream, warm=1, reps=2)
-    same = bool(np.array_equal(ds.cpu().numpy().view(np.uint32), outs.cpu().numpy().view(np.uint32)))
-    emit({"suite": "config4", "problems": len(probs), "points": int(offs[-1]), "d": 16,
-          "pairs": float(sum(float(len(p)) ** 2 for p in probs)),
-          "batched_s": ms_b * 1e-3, "loop_of_single_calls_s": ms_l * 1e-3, "speedup_vs_loop": ms_l / ms_b,
-          "first_call_s_plan_autotune_capture": first_s,
-          "agreement": {"bit_exact_vs_single_calls": same}})
-    ctx.close()
+    batched_case(2048, stream, emit, "config4")
     return 0
 
 
@@ -677,10 +690,30 @@ def run_scaling(args):
     return 1 if failed else 0
 
 
+def run_batched(args):
+    """Config 4's workload alone, with --batched problems (a small count
+    keeps an ncu capture of the batched kernel short)."""
+    import torch
+
+    from culof_gb300 import _culof
+
+    torch.cuda.set_device(0)
+    dev = _culof.device_info()
+
+    def emit(line):
+        line["device"] = dev
+        print(json.dumps(line), flush=True)
+
+    batched_case(args.batched, torch.cuda.current_stream(), emit, "batched")
+    return 0
+
+
 def main():
     args = parse_args()
     if args.suite:
         return run_suite(args)
+    if args.batched:
+        return run_batched(args)
     if args.scaling:
         return run_scaling(args)
     if args.impl == "reference":

@@ -309,8 +309,10 @@ __device__ __forceinline__ void offer_row(RowLists<kBM>& L, int r, const uint64_
 // rows x CP pairs give 2 * CP independent packed FMA chains. Distances are
 // the oracle's direct-difference chain, exactly (per-lane IEEE sub.rn /
 // fma.rn).
+// Two CTAs per SM (what the shared memory allows up to DP = 32); without the
+// minimum, the compiler gives the DP = 8 forms 64 registers and spills.
 template <int DP, int CP>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, DP <= 32 ? 2 : 1)
 batched_knn_kernel(const float* __restrict__ xc, const unsigned* __restrict__ lidx, const int64_t* __restrict__ off,
                    const int* __restrict__ ks, const int64_t* __restrict__ nkoff, const uint2* __restrict__ items,
                    int nitems, int d, unsigned* __restrict__ counter, int32_t* __restrict__ nbr_idx,
@@ -452,24 +454,33 @@ batched_knn_kernel(const float* __restrict__ xc, const unsigned* __restrict__ li
                 for (int h = 0; h < 2; ++h)
 #pragma unroll
                     for (int q = 0; q < CP; ++q) s[h][q] = 0;
+                // dimensions past d are zero in both operands: each adds
+                // fma(0, 0, s) = s, so the chain over all DP equals the
+                // oracle's chain over d
 #pragma unroll
                 for (int f = 0; f < DP; ++f) {
-                    if (f < d) {
-                        const uint64_t a0 = sh.rows2[r][f], a1 = sh.rows2[r + 1][f];
+                    const uint64_t a0 = sh.rows2[r][f], a1 = sh.rows2[r + 1][f];
 #pragma unroll
-                        for (int q = 0; q < CP; ++q) {
-                            uint64_t t0, t1;
-                            asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(t0) : "l"(a0), "l"(cp[q][f]));
-                            asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(t1) : "l"(a1), "l"(cp[q][f]));
-                            s[0][q] = fma2(t0, t0, s[0][q]);
-                            s[1][q] = fma2(t1, t1, s[1][q]);
-                        }
+                    for (int q = 0; q < CP; ++q) {
+                        uint64_t t0, t1;
+                        asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(t0) : "l"(a0), "l"(cp[q][f]));
+                        asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(t1) : "l"(a1), "l"(cp[q][f]));
+                        s[0][q] = fma2(t0, t0, s[0][q]);
+                        s[1][q] = fma2(t1, t1, s[1][q]);
                     }
                 }
 #pragma unroll
                 for (int h = 0; h < 2; ++h) {
                     const int gr = r0 + r + h;
                     if (gr >= n) break;  // warp-uniform
+                    // a key can beat the row's k-th key only if its distance
+                    // is at most the k-th distance: test the distances first
+                    const uint64_t kk = sh.L.kth[r + h];
+                    const float kd = kk == kKeyMax ? __int_as_float(0x7f800000) : __uint_as_float(key_bits(kk));
+                    bool maybe = false;
+#pragma unroll
+                    for (int q = 0; q < CP; ++q) maybe |= (lo_f(s[h][q]) <= kd) | (hi_f(s[h][q]) <= kd);
+                    if (!__any_sync(0xffffffffu, maybe)) continue;
                     uint64_t key[2 * CP];
 #pragma unroll
                     for (int q = 0; q < CP; ++q) {
