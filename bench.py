@@ -59,8 +59,8 @@ PATH_NAMES = ["auto", "fast", "general", "tensor"]
 # very workload (dram__bytes_read.sum + dram__bytes_write.sum); other
 # workloads report null.
 MEASURED_SWEEP_TRAFFIC = {
-    ("clusters", 200_000, 8, 20): (17_980_000 + 74_240_000,
-                                   "ncu: 17.98 MB read + 74.24 MB written per sweep_kernel launch at this workload"),
+    ("clusters", 200_000, 8, 20): (17_030_000 + 10_850_000,
+                                   "ncu: 17.03 MB read + 10.85 MB written per sweep_kernel launch at this workload"),
 }
 
 
