@@ -98,24 +98,37 @@ __device__ __forceinline__ float unflip_float(unsigned k) {
     return __uint_as_float((k & 0x80000000u) ? (k & 0x7FFFFFFFu) : ~k);
 }
 
+// Per dimension f: mm[2f] = min key, mm[2f+1] = max key (flipped floats).
+// One coalesced pass over the n x d values: each thread stays on one
+// dimension (the block's active threads and its stride are multiples of d),
+// reduces in shared memory, and one thread per dimension and block updates
+// the global words. Requires d <= kMaxMinmaxDims.
+constexpr int kMaxMinmaxDims = 256;
 __global__ void minmax_kernel(const float* __restrict__ xc, int64_t n, int d, unsigned* __restrict__ mm) {
-    // mm[2f] = min key, mm[2f+1] = max key (flipped floats)
-    for (int f = 0; f < d; ++f) {
+    __shared__ unsigned slo[kMaxMinmaxDims], shi[kMaxMinmaxDims];
+    for (int f = threadIdx.x; f < d; f += blockDim.x) {
+        slo[f] = 0xFFFFFFFFu;
+        shi[f] = 0u;
+    }
+    __syncthreads();
+    const int per = static_cast<int>(blockDim.x) / d * d;  // active threads
+    if (static_cast<int>(threadIdx.x) < per) {
+        const int f = static_cast<int>(threadIdx.x) % d;
         unsigned lo = 0xFFFFFFFFu, hi = 0u;
-        for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
-             i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-            const unsigned k = flip_float(xc[i * d + f]);
+        const int64_t total = n * d;
+        for (int64_t t = static_cast<int64_t>(blockIdx.x) * per + threadIdx.x; t < total;
+             t += static_cast<int64_t>(gridDim.x) * per) {
+            const unsigned k = flip_float(xc[t]);
             lo = min(lo, k);
             hi = max(hi, k);
         }
-        for (int o = 16; o > 0; o >>= 1) {
-            lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
-            hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
-        }
-        if ((threadIdx.x & 31) == 0) {
-            atomicMin(&mm[2 * f], lo);
-            atomicMax(&mm[2 * f + 1], hi);
-        }
+        atomicMin(&slo[f], lo);
+        atomicMax(&shi[f], hi);
+    }
+    __syncthreads();
+    for (int f = threadIdx.x; f < d; f += blockDim.x) {
+        atomicMin(&mm[2 * f], slo[f]);
+        atomicMax(&mm[2 * f + 1], shi[f]);
     }
 }
 
@@ -194,17 +207,27 @@ __global__ void sort_upsweep_kernel(const unsigned* __restrict__ keys, int64_t n
     counts[static_cast<int64_t>(threadIdx.x) * nblocks + blockIdx.x] = hist[threadIdx.x];
 }
 
-// Exclusive scan of counts[256 * nblocks] in digit-major order (one block).
+// Exclusive scan of counts[256 * nblocks] in digit-major order (one block):
+// each thread scans kScanItems consecutive counts per step, the block scans
+// the threads' totals.
+constexpr int kScanItems = 8;
 __global__ void sort_scan_kernel(unsigned* __restrict__ counts, int64_t len) {
     __shared__ unsigned warp_tot[32];
     __shared__ unsigned carry;
     if (threadIdx.x == 0) carry = 0;
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int64_t base = 0; base < len; base += blockDim.x) {
-        const int64_t i = base + threadIdx.x;
-        const unsigned v = i < len ? counts[i] : 0u;
-        unsigned x = v;
+    const int64_t step = static_cast<int64_t>(blockDim.x) * kScanItems;
+    for (int64_t base = 0; base < len; base += step) {
+        const int64_t i0 = base + static_cast<int64_t>(threadIdx.x) * kScanItems;
+        unsigned v[kScanItems];
+        unsigned tsum = 0;
+#pragma unroll
+        for (int j = 0; j < kScanItems; ++j) {
+            v[j] = i0 + j < len ? counts[i0 + j] : 0u;
+            tsum += v[j];
+        }
+        unsigned x = tsum;
         for (int o = 1; o < 32; o <<= 1) {
             const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
             if (lane >= o) x += y;
@@ -220,10 +243,14 @@ __global__ void sort_scan_kernel(unsigned* __restrict__ counts, int64_t len) {
             warp_tot[lane] = w;
         }
         __syncthreads();
-        const unsigned before = (warp > 0 ? warp_tot[warp - 1] : 0u) + carry;
-        if (i < len) counts[i] = before + x - v;
+        unsigned run = (warp > 0 ? warp_tot[warp - 1] : 0u) + carry + x - tsum;
+#pragma unroll
+        for (int j = 0; j < kScanItems; ++j) {
+            if (i0 + j < len) counts[i0 + j] = run;
+            run += v[j];
+        }
         __syncthreads();
-        if (threadIdx.x == blockDim.x - 1) carry = before + x;
+        if (threadIdx.x == blockDim.x - 1) carry = run;
         __syncthreads();
     }
 }
@@ -1093,7 +1120,7 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
     unsigned* vals = perm_.as<unsigned>(2 * static_cast<size_t>(n));
     minmax_init_kernel<<<1, 32, 0, s>>>(mm, d);
     CG_LAUNCH_CHECK();
-    minmax_kernel<<<grid_for(n, 256), 256, 0, s>>>(xc, n, d, mm);
+    minmax_kernel<<<grid_for(n * d, 256), 256, 0, s>>>(xc, n, d, mm);
     CG_LAUNCH_CHECK();
     select_dims_kernel<<<1, 32, 0, s>>>(mm, d, dims);
     CG_LAUNCH_CHECK();

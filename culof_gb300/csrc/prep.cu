@@ -44,15 +44,26 @@ __global__ void center_partials_kernel(const float* __restrict__ x, int64_t n, i
     partial[t] = s;
 }
 
-// One thread per feature: sum the partials in chunk order.
-// mode 0 -> mean[f]; mode 1 -> inv_std[f] (population std; 1 for sd <= 1e-12).
+// One block per feature: the feature's partials are staged in shared memory
+// (the whole block loads, many loads in flight), then one thread sums them in
+// chunk order. mode 0 -> mean[f]; mode 1 -> inv_std[f] (population std; 1 for
+// sd <= 1e-12).
+constexpr int kFinalizeBuf = 4096;
 __global__ void center_finalize_kernel(const double* __restrict__ partial, int64_t chunks,
                                        int d, int64_t n, int mode, double* __restrict__ mean,
                                        double* __restrict__ inv_std) {
-    const int f = blockIdx.x * blockDim.x + threadIdx.x;
-    if (f >= d) return;
+    __shared__ double buf[kFinalizeBuf];
+    const int f = blockIdx.x;
     double total = 0.0;
-    for (int64_t c = 0; c < chunks; ++c) total = __dadd_rn(total, partial[c * d + f]);
+    for (int64_t c0 = 0; c0 < chunks; c0 += kFinalizeBuf) {
+        const int m = static_cast<int>(chunks - c0 < kFinalizeBuf ? chunks - c0 : kFinalizeBuf);
+        for (int i = threadIdx.x; i < m; i += blockDim.x) buf[i] = partial[(c0 + i) * d + f];
+        __syncthreads();
+        if (threadIdx.x == 0)
+            for (int i = 0; i < m; ++i) total = __dadd_rn(total, buf[i]);
+        __syncthreads();
+    }
+    if (threadIdx.x != 0) return;
     const double dn = static_cast<double>(n);
     if (mode == 0) {
         mean[f] = __ddiv_rn(total, dn);
@@ -116,14 +127,12 @@ void center(const float* x, int64_t n, int d, bool normalize, float* xc, double*
     const int pgrid = static_cast<int>(ceil_div(items, block));
     center_partials_kernel<<<pgrid, block, 0, s>>>(x, n, d, nullptr, partial);
     CG_LAUNCH_CHECK();
-    center_finalize_kernel<<<static_cast<int>(ceil_div(d, 128)), 128, 0, s>>>(partial, chunks, d, n, 0,
-                                                                                mean, inv_std);
+    center_finalize_kernel<<<d, 256, 0, s>>>(partial, chunks, d, n, 0, mean, inv_std);
     CG_LAUNCH_CHECK();
     if (normalize) {
         center_partials_kernel<<<pgrid, block, 0, s>>>(x, n, d, mean, partial);
         CG_LAUNCH_CHECK();
-        center_finalize_kernel<<<static_cast<int>(ceil_div(d, 128)), 128, 0, s>>>(partial, chunks, d, n,
-                                                                                    1, mean, inv_std);
+        center_finalize_kernel<<<d, 256, 0, s>>>(partial, chunks, d, n, 1, mean, inv_std);
         CG_LAUNCH_CHECK();
     }
     center_apply_kernel<<<grid_for(n * d, 256), 256, 0, s>>>(x, n, d, mean, inv_std, xc);
