@@ -1091,11 +1091,12 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
         if (wide) {
             nsplit = choose_splits(nt, sms);
         } else if (!tensor) {
-            // small-d sweep: about 8 waves of CTAs (2 per SM); more splits
-            // only add merge work and restart more rows from the seed
-            // (n = 100k: 3 splits 3.33 ms against 7 splits 3.73 ms; n = 200k:
-            // 2 splits 8.85 ms against 4 splits 9.15 ms)
-            nsplit = (16 * sms + nt / 2) / nt;
+            // small-d sweep: about 9 waves of CTAs (2 per SM); more splits
+            // only add merge work and restart more rows from the seed, fewer
+            // leave the tail unbalanced (measured best: 7 splits at n = 50k,
+            // 3 at 100k (3.33 ms against 3.73 ms with 7), 2 at 200k (8.85 ms
+            // against 9.15 ms with 4))
+            nsplit = (18 * sms + nt / 2) / nt;
             nsplit = nsplit < 1 ? 1 : nsplit > 7 ? 7 : nsplit;
         } else if (nt < 4 * sms) {
             nsplit = (4 * sms + nt / 2) / nt;
