@@ -133,7 +133,16 @@ int Engine::choose_path(int64_t n, int d, int k) const {
         throw Error(kInvalidArgument, "fused path requested but unsupported for this n/d/k");
     if (p == kPathFast || p == kPathTensor) return p;
     if (!ok) return kPathGeneral;
-    return d > 8 ? kPathTensor : kPathFast;
+    if (d <= 8) return kPathFast;
+    // 8 < d <= 16 with fewer row tiles than one wave of tensor CTAs (two per
+    // SM): the FP32 wide sweep is as fast or faster on every input measured
+    // (n = 20k: 1.8 ms against 1.85-2.8 ms on clustered, mixture and
+    // low-rank data); beyond that the tensor path wins or ties
+    int sms = 0;
+    CG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_));
+    const int64_t nt = (n + 127) / 128;
+    if (d <= 16 && nt < 2 * static_cast<int64_t>(sms)) return kPathFast;
+    return kPathTensor;
 }
 
 void Engine::knn_general(const float* xc, const float* norms, int64_t n, int d, int k,

@@ -114,6 +114,11 @@ def test_auto_selects_the_fast_path_for_small_d(ctx):
     assert ctx.last_path() == _culof.PATH_GENERAL
     ctx.lof(synthetic.reference_test_data(600, 32, seed=5), 20)
     assert ctx.last_path() == _culof.PATH_TENSOR
+    # 8 < d <= 16: the FP32 wide sweep below one wave of tensor CTAs, else the tensor path
+    ctx.lof(synthetic.reference_test_data(600, 12, seed=5), 20)
+    assert ctx.last_path() == _culof.PATH_FAST
+    ctx.lof(synthetic.clusters_with_outliers(40_000, 16, seed=5), 20)
+    assert ctx.last_path() == _culof.PATH_TENSOR
     ctx.lof(synthetic.reference_test_data(600, 200, seed=5), 20)
     assert ctx.last_path() == _culof.PATH_GENERAL
 
