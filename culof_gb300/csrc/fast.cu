@@ -1206,7 +1206,11 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
     int* pcount = nullptr;
     const unsigned* order = nullptr;
     constexpr int kMaxListTiles = 16384;  // lists take nt^2 x 8 bytes: up to 2 GiB
-    if (!wide && !tensor && sweep && nt <= kMaxListTiles) {
+    // CULOF_PRUNE_LISTS=0 walks the whole spiral as inputs above the list
+    // limit do (the same results; it puts that path within reach of tests)
+    const char* lists_env = std::getenv("CULOF_PRUNE_LISTS");
+    const bool lists_on = !(lists_env && lists_env[0] == '0');
+    if (!wide && !tensor && sweep && nt <= kMaxListTiles && lists_on) {
         plist = plist_.as<uint2>(static_cast<size_t>(nt) * nt);
         pcount = pcount_.as<int>(nt);
         switch (dp) {

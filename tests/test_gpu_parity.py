@@ -106,6 +106,22 @@ def test_knn_bit_exact_vs_oracle(ctx, path, name, make, k):
     np.testing.assert_array_equal(d2.view(np.uint32), o_d2.view(np.uint32))
 
 
+@pytest.mark.parametrize("name", ["clusters", "ragged", "k64", "n385_k64", "d1", "dups_heavy"])
+def test_knn_without_prune_lists_bit_exact(ctx, monkeypatch, name):
+    # inputs above 16,384 row tiles sweep the whole spiral without per-tile
+    # candidate lists; CULOF_PRUNE_LISTS=0 takes that path at any size
+    monkeypatch.setenv("CULOF_PRUNE_LISTS", "0")
+    make, k = {c[0]: (c[1], c[2]) for c in KNN_CASES}[name]
+    X = make()
+    ctx.set_path(_culof.PATH_FAST)
+    idx, d2, kd = run_knn(ctx, X, k)
+    Xc, _, _ = oracle.center(X)
+    o_idx, o_d2, o_kd = oracle.knn(Xc, k)
+    np.testing.assert_array_equal(kd.view(np.uint32), o_kd.view(np.uint32))
+    np.testing.assert_array_equal(idx, o_idx)
+    np.testing.assert_array_equal(d2.view(np.uint32), o_d2.view(np.uint32))
+
+
 def test_auto_selects_the_fast_path_for_small_d(ctx):
     X = synthetic.clusters_with_outliers(3000, 8, seed=1)
     ctx.lof(X, 20)
