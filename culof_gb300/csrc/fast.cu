@@ -633,7 +633,7 @@ sweep_kernel(const float* __restrict__ tiles, int nt, int qs, int nsplit, int k,
              const unsigned* __restrict__ max_norm_bits,
              unsigned long long* __restrict__ kth_shared, uint64_t* __restrict__ partial, int* __restrict__ status,
              unsigned long long* __restrict__ evaluated_blocks, const uint2* __restrict__ plist,
-             const int* __restrict__ pcount, const unsigned* __restrict__ order) {
+             const int* __restrict__ pcount, const unsigned* __restrict__ order, const float* __restrict__ boxes) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     SweepSmem<DP, M>& sh = *reinterpret_cast<SweepSmem<DP, M>*>(smem_raw);
     // row tiles with the longest candidate lists first (tail balance)
@@ -752,8 +752,18 @@ sweep_kernel(const float* __restrict__ tiles, int nt, int qs, int nsplit, int k,
                     t = static_cast<int>(e.x);
                     pass = !(__fmul_rd(__uint_as_float(e.y), kPruneShrink) > kmax);
                 } else {
+                    // no list: the tile's own box (global array, the
+                    // list builder's rounded-down gap) against the CTA box
                     t = spiral_tile(T, qs + split + nsplit * j, nt);
-                    pass = true;
+                    const float* b = boxes + static_cast<int64_t>(t) * 2 * DP;
+                    float g2 = 0.0f;
+#pragma unroll 1
+                    for (int f = 0; f < DP; ++f) {  // rolled: the row registers are live here
+                        const float gap =
+                            fmaxf(0.0f, fmaxf(__fsub_rd(b[f], sh.cbox[1][f]), __fsub_rd(sh.cbox[0][f], b[DP + f])));
+                        g2 = __fadd_rd(g2, __fmul_rd(gap, gap));
+                    }
+                    pass = !(__fmul_rd(g2, kPruneShrink) > kmax);
                 }
             }
             const unsigned mk = __ballot_sync(0xffffffffu, pass);
@@ -1017,11 +1027,11 @@ template <int DP, int M>
 void launch_sweep(const float* tiles, int nt, int qs, int nsplit, int k, const unsigned* maxn,
                   unsigned long long* kth_shared,
                   uint64_t* partial, int* status, unsigned long long* evaluated, const uint2* plist, const int* pcount,
-                  const unsigned* order, cudaStream_t s) {
+                  const unsigned* order, const float* boxes, cudaStream_t s) {
     const size_t smem = sizeof(SweepSmem<DP, M>);
     set_max_dynamic_smem(reinterpret_cast<const void*>(sweep_kernel<DP, M>), static_cast<int>(smem));
     sweep_kernel<DP, M><<<nt * nsplit, kThreads, smem, s>>>(tiles, nt, qs, nsplit, k, maxn, kth_shared, partial,
-                                                            status, evaluated, plist, pcount, order);
+                                                            status, evaluated, plist, pcount, order, boxes);
     CG_LAUNCH_CHECK();
 }
 
@@ -1247,9 +1257,9 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
         const bool big = k > 32;
 #define CG_SWEEP(DPV)                                                                                 \
     (big ? launch_sweep<DPV, 96>(tiles, nt, qs, nsplit, k, maxn, kth_shared, partial, status, evaluated, plist, pcount, \
-                                 order, s)                                                                         \
+                                 order, boxes, s)                                                                  \
          : launch_sweep<DPV, 64>(tiles, nt, qs, nsplit, k, maxn, kth_shared, partial, status, evaluated, plist, pcount, \
-                                 order, s))
+                                 order, boxes, s))
         switch (dp) {
             case 2: CG_SWEEP(2); break;
             case 4: CG_SWEEP(4); break;
