@@ -139,20 +139,23 @@ __global__ void __launch_bounds__(256) tc_seed_kernel(const float* __restrict__ 
     for (int r = warp; r < kRT; r += nw) {
         const int64_t pos = base + r;
         const bool row_valid = idx[r] != kNoIndex;
+        // the lane's four columns as four independent chains (each in the
+        // oracle's order), the row's coordinate loaded once per dimension
+        float s4[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll 4
+        for (int f = 0; f < d; ++f) {
+            const float a = spts[r * ld + f];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const float t = __fsub_rn(a, spts[(j * 32 + lane) * ld + f]);
+                s4[j] = __fmaf_rn(t, t, s4[j]);
+            }
+        }
         uint64_t v[4];
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             const int c = j * 32 + lane;
-            uint64_t key = kKeyMax;
-            if (row_valid && c != r && idx[c] != kNoIndex) {
-                float s = 0.0f;
-                for (int f = 0; f < d; ++f) {
-                    const float t = __fsub_rn(spts[r * ld + f], spts[c * ld + f]);
-                    s = __fmaf_rn(t, t, s);
-                }
-                key = make_key(__float_as_uint(s), idx[c]);
-            }
-            v[j] = key;
+            v[j] = (row_valid && c != r && idx[c] != kNoIndex) ? make_key(__float_as_uint(s4[j]), idx[c]) : kKeyMax;
         }
         warp_bitonic_sort<4>(v);
 #pragma unroll
