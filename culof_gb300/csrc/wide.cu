@@ -66,20 +66,23 @@ __global__ void __launch_bounds__(kThreads) wide_seed_kernel(const float* __rest
     for (int r = warp; r < kRT; r += kWarps) {
         const int64_t pos = static_cast<int64_t>(T) * kRT + r;
         const bool row_valid = idx[r] != kNoIndex;
+        // the lane's four columns as four independent chains (each in the
+        // oracle's order), the row's coordinate loaded once per dimension
+        float s4[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll 4
+        for (int f = 0; f < d; ++f) {
+            const float a = stile[f * kCT + r];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const float t = __fsub_rn(a, stile[f * kCT + j * 32 + lane]);
+                s4[j] = __fmaf_rn(t, t, s4[j]);
+            }
+        }
         uint64_t v[4];
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             const int c = j * 32 + lane;
-            uint64_t key = kKeyMax;
-            if (row_valid && c != r && idx[c] != kNoIndex) {
-                float s = 0.0f;
-                for (int f = 0; f < d; ++f) {
-                    const float t = __fsub_rn(stile[f * kCT + r], stile[f * kCT + c]);
-                    s = __fmaf_rn(t, t, s);
-                }
-                key = make_key(__float_as_uint(s), idx[c]);
-            }
-            v[j] = key;
+            v[j] = (row_valid && c != r && idx[c] != kNoIndex) ? make_key(__float_as_uint(s4[j]), idx[c]) : kKeyMax;
         }
         warp_bitonic_sort<4>(v);
 #pragma unroll
