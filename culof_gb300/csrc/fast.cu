@@ -518,7 +518,62 @@ __global__ void __launch_bounds__(kThreads) seed_kernel(const float* __restrict_
             const uint64_t t = __shfl_sync(0xffffffffu, v[j], owner);
             if (j == oreg) kk = t;
         }
-        if (row_valid && qs > 1) {
+        if (row_valid && qs > 1 && k <= 32) {
+            // neighbour tiles, k <= 32: the 32 best so far stay in one
+            // register across the warp (sorted); keys below the current k-th
+            // key gather in shared memory, 32 at most, and join by a bitonic
+            // merge in registers
+            uint64_t best = v[0];
+            float ra[DP];
+#pragma unroll
+            for (int f = 0; f < DP; ++f) ra[f] = tile_coord<DP>(tile[0], r, f);
+            int cnt = 0;
+            const auto merge_pending = [&]() {
+                uint64_t w[1] = {lane < cnt ? lst[lane] : kKeyMax};
+                warp_bitonic_sort<1>(w);
+                // the 32 smallest of both sorted runs, as a bitonic sequence,
+                // then sorted by half-cleaners
+                const uint64_t rev = __shfl_sync(0xffffffffu, w[0], 31 - lane);
+                uint64_t c = best < rev ? best : rev;
+#pragma unroll
+                for (int st = 16; st > 0; st >>= 1) {
+                    const uint64_t o = shfl_xor_u64(c, st);
+                    c = (lane & st) == 0 ? (o < c ? o : c) : (o > c ? o : c);
+                }
+                best = c;
+                kk = __shfl_sync(0xffffffffu, best, k - 1);
+                cnt = 0;
+            };
+            for (int q = 1; q < qs; ++q) {
+                const unsigned* idq = reinterpret_cast<const unsigned*>(tile[q] + tile_index_off(DP));
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const int c = j * 32 + lane;
+                    float d2 = 0.0f;  // tile_dist2's arithmetic, row coordinates in registers
+#pragma unroll
+                    for (int f = 0; f < DP; ++f) {
+                        const float t = __fsub_rn(ra[f], tile_coord<DP>(tile[q], c, f));
+                        d2 = __fmaf_rn(t, t, d2);
+                    }
+                    const uint64_t key = idq[c] != kNoIndex ? make_key(__float_as_uint(d2), idq[c]) : kKeyMax;
+                    unsigned m = __ballot_sync(0xffffffffu, key < kk);
+                    if (m && cnt + __popc(m) > 32) {
+                        __syncwarp();
+                        merge_pending();
+                        __syncwarp();
+                        m = __ballot_sync(0xffffffffu, key < kk);
+                    }
+                    if (m) {
+                        if (key < kk) lst[cnt + __popc(m & ((1u << lane) - 1u))] = key;
+                        cnt += __popc(m);
+                    }
+                }
+            }
+            __syncwarp();
+            if (cnt > 0) merge_pending();
+            if (lane < k) seed_keys[pos * k + lane] = best;
+            __syncwarp();
+        } else if (row_valid && qs > 1) {
             // neighbour tiles: append the keys below the current k-th key and
             // merge them into the sorted k best (at most 32 at a time)
 #pragma unroll
