@@ -500,7 +500,7 @@ __global__ void __launch_bounds__(kThreads) seed_kernel(const float* __restrict_
     for (int r = warp; r < kRT; r += kWarps) {
         const int64_t pos = static_cast<int64_t>(T) * kRT + r;
         const bool row_valid = idx[r] != kNoIndex;
-        // own tile: sort all 128 keys
+        // own tile: its 128 keys (the k best of them sorted below)
         uint64_t v[4];
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
@@ -510,20 +510,37 @@ __global__ void __launch_bounds__(kThreads) seed_kernel(const float* __restrict_
                 key = make_key(__float_as_uint(tile_dist2<DP>(tile[0], r, tile[0], c)), idx[c]);
             v[j] = key;
         }
-        warp_bitonic_sort<4>(v);
-        const int owner = (k - 1) & 31, oreg = (k - 1) >> 5;
         uint64_t kk = kKeyMax;
+        uint64_t best = kKeyMax;  // k <= 32: the 32 best so far, sorted across the warp
+        if (k <= 32) {
+            // the first 32 keys sorted, the other three registers merged in
+            // (those with a key below the current k-th key)
+            uint64_t w[1] = {v[0]};
+            warp_bitonic_sort<1>(w);
+            best = w[0];
+            kk = __shfl_sync(0xffffffffu, best, k - 1);
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const uint64_t t = __shfl_sync(0xffffffffu, v[j], owner);
-            if (j == oreg) kk = t;
+            for (int j = 1; j < 4; ++j) {
+                if (!__any_sync(0xffffffffu, v[j] < kk)) continue;
+                uint64_t x[1] = {v[j] < kk ? v[j] : kKeyMax};
+                warp_bitonic_sort<1>(x);
+                best = warp_merge_lowest32(best, x[0]);
+                kk = __shfl_sync(0xffffffffu, best, k - 1);
+            }
+        } else {
+            warp_bitonic_sort<4>(v);
+            const int owner = (k - 1) & 31, oreg = (k - 1) >> 5;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const uint64_t t = __shfl_sync(0xffffffffu, v[j], owner);
+                if (j == oreg) kk = t;
+            }
         }
         if (row_valid && qs > 1 && k <= 32) {
             // neighbour tiles, k <= 32: the 32 best so far stay in one
             // register across the warp (sorted); keys below the current k-th
             // key gather in shared memory, 32 at most, and join by a bitonic
             // merge in registers
-            uint64_t best = v[0];
             float ra[DP];
 #pragma unroll
             for (int f = 0; f < DP; ++f) ra[f] = tile_coord<DP>(tile[0], r, f);
@@ -531,16 +548,7 @@ __global__ void __launch_bounds__(kThreads) seed_kernel(const float* __restrict_
             const auto merge_pending = [&]() {
                 uint64_t w[1] = {lane < cnt ? lst[lane] : kKeyMax};
                 warp_bitonic_sort<1>(w);
-                // the 32 smallest of both sorted runs, as a bitonic sequence,
-                // then sorted by half-cleaners
-                const uint64_t rev = __shfl_sync(0xffffffffu, w[0], 31 - lane);
-                uint64_t c = best < rev ? best : rev;
-#pragma unroll
-                for (int st = 16; st > 0; st >>= 1) {
-                    const uint64_t o = shfl_xor_u64(c, st);
-                    c = (lane & st) == 0 ? (o < c ? o : c) : (o > c ? o : c);
-                }
-                best = c;
+                best = warp_merge_lowest32(best, w[0]);
                 kk = __shfl_sync(0xffffffffu, best, k - 1);
                 cnt = 0;
             };
@@ -614,6 +622,8 @@ __global__ void __launch_bounds__(kThreads) seed_kernel(const float* __restrict_
             if (cnt > k) cnt = merge_sorted_prefix<1>(lst, k, cnt, k, k - 1, exact, &kk);
             for (int e = lane; e < k; e += 32) seed_keys[pos * k + e] = lst[e];
             __syncwarp();
+        } else if (k <= 32) {
+            if (lane < k) seed_keys[pos * k + lane] = best;
         } else {
 #pragma unroll
             for (int j = 0; j < 4; ++j) {

@@ -49,6 +49,21 @@ __device__ __forceinline__ void warp_bitonic_sort(uint64_t (&v)[E]) {
     }
 }
 
+// The 32 smallest of two ascending 32-key runs a and b (one key per lane,
+// element = lane), ascending: the elementwise minimum of a and reversed b is
+// a bitonic sequence holding them, and five half-cleaner steps sort it.
+__device__ __forceinline__ uint64_t warp_merge_lowest32(uint64_t a, uint64_t b) {
+    const int lane = threadIdx.x & 31;
+    const uint64_t rb = __shfl_sync(0xffffffffu, b, 31 - lane);
+    uint64_t c = a < rb ? a : rb;
+#pragma unroll
+    for (int st = 16; st > 0; st >>= 1) {
+        const uint64_t o = shfl_xor_u64(c, st);
+        c = (lane & st) == 0 ? (o < c ? o : c) : (o > c ? o : c);
+    }
+    return c;
+}
+
 // After warp_bitonic_sort: flags the first copy of every distinct key that
 // is not `sentinel`, returns the rank of each kept element among kept ones
 // (or -1) and the number kept.
