@@ -13,11 +13,10 @@ offset and the labels.
   buffers: host->device copy of X, the pipeline and the device->host copy of
   nof + labels + offset, every step (wall time of the synchronous call).
 * roofline: the distance sweep kernel (the dominant kernel): the algorithmic
-  work, 2d FLOP for each of the n (n - 384) pairs outside the rows' seed
-  windows (the own tile and its two Morton neighbour tiles, which the seed
-  kernel covers; one evaluation per pair), over its event time, against the
-  measured FP32
-  FMA peak. The kernel skips column tiles that a bounding-box test proves
+  work, 2d FLOP for each of the n (n - 640) pairs outside the rows' seed
+  windows (the own tile and its four nearest Morton neighbour tiles, which
+  the seed kernel covers; one evaluation per pair), over its event time,
+  against the measured FP32 FMA peak. The kernel skips column tiles that a bounding-box test proves
   farther than every k-th neighbour; the pairs it actually evaluated, the
   pruned fraction and its FLOP rate on the evaluated pairs are reported
   beside it (executed_tflops, executed_frac).
@@ -394,10 +393,10 @@ def run_ours(args):
     stages = {name: statistics.mean(v) for name, v in stage_acc.items()}
     fp32_peak = max(_culof.probe_fp32_tflops(True), _culof.probe_fp32_tflops(False))
     # the sweep evaluates every pair outside the rows' seed window: the own
-    # 128-point tile (tensor and wide paths), or the own tile and its two
-    # Morton neighbour tiles (small-d path, d <= 8)
+    # 128-point tile (tensor and wide paths), or the own tile and its four
+    # nearest Morton neighbour tiles (small-d path, d <= 8)
     nt = (n + 127) // 128
-    window = min(nt, 3) if (ctx.last_path() == _culof.PATH_FAST and d <= 8) else 1
+    window = min(nt, 5) if (ctx.last_path() == _culof.PATH_FAST and d <= 8) else 1
     sweep_pairs = float(n) * float(n - min(n, 128 * window)) if nt > window else 0.0
     sweep_ms = stages.get("sweep")
     roofline = None

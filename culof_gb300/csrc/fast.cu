@@ -48,7 +48,7 @@ using namespace sweep;
 constexpr int kPairs = kCT / 2;
 constexpr int kRowsPerLane = 4;
 constexpr int kStages = 4;     // column tiles in flight
-constexpr int kSeedWindow = 3;  // tiles of the seed: T, T+1, T-1
+constexpr int kSeedWindow = 5;  // tiles of the seed: T, T+1, T-1, T+2, T-2
 constexpr int kMaxDP = 8;      // the small-d sweep; wider points take wide.cu's
 constexpr int kMaxWideD = 128;
 constexpr int kMortonDims = 8;  // Morton key over (up to) the 8 widest dimensions
@@ -347,7 +347,7 @@ __device__ __forceinline__ float tile_dist2(const float* ta, int ca, const float
 // kKeyMax padded) and its k-th key, the starting point of the row's shared
 // k-th key (kth_shared) that the sweep CTAs tighten with atomicMin. The
 // window is the first qs spiral positions: tile T itself and its Morton
-// neighbours T+1 and T-1, whose points start the k-th distances much closer
+// neighbours T+1, T-1, T+2 and T-2, whose points start the k-th distances much closer
 // to their final values than tile T alone (fewer candidates reach the
 // sweep's lists); the sweep covers the spiral from position qs on.
 // Pruning margin: the float32 direct-difference distance D of two points at

@@ -115,7 +115,7 @@ CULOF_API unsigned long long culof_kernel_launch_count(void);
 /* Row x column pairs the last small-d FP32 sweep of this context evaluated
  * (tiles that a bounding-box test proves farther than every k-th neighbour
  * are skipped) and the pairs it would evaluate without that test (every
- * column tile past the seed's own and two neighbour tiles); both 0 after
+ * column tile past the seed's own and four neighbour tiles); both 0 after
  * other paths. Synchronises the context stream. */
 CULOF_API int culof_context_pair_stats(culof_context* ctx, double* evaluated_pairs, double* total_pairs);
 

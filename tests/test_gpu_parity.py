@@ -75,8 +75,8 @@ KNN_CASES = [
     ("k64", lambda: synthetic.clusters_with_outliers(5000, 8, seed=23), 64),
     ("k33_d3", lambda: synthetic.clusters_with_outliers(3000, 3, seed=24), 33),
     ("d1", lambda: synthetic.clusters_with_outliers(2000, 1, seed=25), 10),
-    # the small-d seed covers tiles T, T+1, T-1: three tiles leave the sweep
-    # nothing; four leave it one tile per row tile
+    # the small-d seed covers tiles T, T+1, T-1, T+2, T-2: three to five
+    # tiles leave the sweep nothing; six leave it one tile per row tile
     ("n300_seed_only", lambda: synthetic.clusters_with_outliers(300, 8, seed=29), 20),
     ("n385_k64", lambda: synthetic.clusters_with_outliers(385, 6, seed=30), 64),
     # the wide-point sweep: d not a multiple of 16, d = 128 with k = 50
@@ -254,14 +254,14 @@ def test_lrd_and_score_stage_entry_points():
 
 @pytest.mark.parametrize("n,swept", [(20_000, True), (300, False)])
 def test_pair_stats_cover_the_sweep_past_the_seed_window(ctx, n, swept):
-    # the small-d seed covers tiles T, T+1, T-1; the sweep every later tile
+    # the small-d seed covers tiles T and T+-1, T+-2; the sweep every later tile
     X = synthetic.clusters_with_outliers(n, 8, seed=31)
     ctx.set_path(_culof.PATH_FAST)
     ctx.lof(X, 20)
     ev, tot = ctx.pair_stats()
     nt = (n + 127) // 128
     if swept:
-        assert tot == nt * (nt - 3) * 128 * 128
+        assert tot == nt * (nt - 5) * 128 * 128
         assert 0 < ev <= tot
     else:
         assert ev == 0 and tot == 0
