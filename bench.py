@@ -58,8 +58,8 @@ PATH_NAMES = ["auto", "fast", "general", "tensor"]
 # very workload (dram__bytes_read.sum + dram__bytes_write.sum); other
 # workloads report null.
 MEASURED_SWEEP_TRAFFIC = {
-    ("clusters", 200_000, 8, 20): (17_030_000 + 10_850_000,
-                                   "ncu: 17.03 MB read + 10.85 MB written per sweep_kernel launch at this workload"),
+    ("clusters", 200_000, 8, 20): (17_140_000 + 11_910_000,
+                                   "ncu: 17.14 MB read + 11.91 MB written per sweep_kernel launch at this workload"),
 }
 
 

@@ -74,6 +74,8 @@ KNN_CASES = [
     ("n129", lambda: synthetic.clusters_with_outliers(129, 8, seed=22), 20),
     ("k64", lambda: synthetic.clusters_with_outliers(5000, 8, seed=23), 64),
     ("k33_d3", lambda: synthetic.clusters_with_outliers(3000, 3, seed=24), 33),
+    # the small-d seed keeps the 32 best in registers for k <= 32
+    ("k32", lambda: synthetic.clusters_with_outliers(2500, 8, seed=32), 32),
     ("d1", lambda: synthetic.clusters_with_outliers(2000, 1, seed=25), 10),
     # the small-d seed covers tiles T, T+1, T-1, T+2, T-2: three to five
     # tiles leave the sweep nothing; six leave it one tile per row tile
