@@ -88,9 +88,10 @@ def parse_args():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--path", choices=["auto", "fast", "general", "tensor"], default="auto")
     p.add_argument("--suite", action="store_true",
-                   help="report harness: one JSON line per benchmark configuration (0-4) with an agreement gate")
+                   help="report harness: one JSON line per benchmark workload (five) with an agreement gate")
     p.add_argument("--batched", type=int, default=0, metavar="N",
-                   help="config 4's batched workload alone with N problems (batched call against single calls)")
+                   help="the batched problem mix (d = 16, k 10-40, n log-uniform in [128, 16384]) with N problems, "
+                        "batched call against single calls")
     p.add_argument("--scaling", action="store_true",
                    help="the reference benchmark's n and d sweeps through culof_gb300.lof, gated bit-exact on the oracle")
     p.add_argument("--workload", choices=["clusters", "factor", "mixture"], default="clusters",
@@ -512,7 +513,7 @@ def _time_calls(fn, stream, warm=2, reps=5):
 
 
 def batched_case(count, stream, emit, label):
-    """Config 4's workload with `count` problems: one batched call (CUDA
+    """The batched problem mix with `count` problems: one batched call (CUDA
     graph replay after the first call) against a loop of single calls, and
     the scores of both compared bit for bit."""
     import torch
@@ -550,7 +551,7 @@ def batched_case(count, stream, emit, label):
 
 
 def run_suite(args):
-    """One JSON line per benchmark configuration, each with its timing and an
+    """One JSON line per benchmark workload, each with its timing and an
     agreement gate against the oracle or an independent exact path (the
     speed and accuracy columns come from the same run)."""
     import torch
@@ -600,20 +601,20 @@ def run_suite(args):
         ctx.close()
         return res, nof.cpu().numpy()
 
-    # config 0 and 1: clusters, d = 8, k = 20, c = 0.01
-    for name, n in (("config0", 20_000), ("config1", 200_000)):
+    # clusters, d = 8, k = 20, c = 0.01, at n = 20k and 200k
+    for name, n in (("clusters_n20000_d8_k20", 20_000), ("clusters_n200000_d8_k20", 200_000)):
         X = synthetic.clusters_with_outliers(n, 8, seed=1)
         res, _ = fit_predict_case(name, X, 20, 0.01, 0, 2000)
         emit(res)
-    # config 2: factor model, d = 128, k = 50: tensor path against the FP32 sweep
+    # factor model, n = 200k, d = 128, k = 50: tensor path against the FP32 sweep
     X = synthetic.factor_model(200_000, 128, seed=1)
-    tres, tnof = fit_predict_case("config2", X, 50, 0.01, 3, 500)
-    fres, fnof = fit_predict_case("config2_fp32", X, 50, 0.01, 1, 1)
+    tres, tnof = fit_predict_case("factor_n200000_d128_k50", X, 50, 0.01, 3, 500)
+    fres, fnof = fit_predict_case("factor_n200000_d128_k50_fp32", X, 50, 0.01, 1, 1)
     tres["fp32_fit_predict_s"] = fres["fit_predict_s"]
     tres["speedup_vs_fp32"] = fres["fit_predict_s"] / tres["fit_predict_s"]
     tres["agreement"]["nof_bit_exact_vs_fp32_path"] = bool(np.array_equal(tnof.view(np.uint32), fnof.view(np.uint32)))
     emit(tres)
-    # config 3: sparse backward, n = 50,000, d = 32, k = 20
+    # sparse backward, mixture, n = 50,000, d = 32, k = 20
     from culof_gb300.autograd import lof_scores
 
     X = synthetic.gradient_mixture(50_000, 32, seed=1)
@@ -637,11 +638,11 @@ def run_suite(args):
     X64 = Xt.double().requires_grad_(True)
     (ob.lof_fixed(X64, idx.long(), False) * w).sum().backward()
     rel = float((g - X64.grad).abs().max() / X64.grad.abs().max())
-    emit({"suite": "config3", "n": len(X), "d": 32, "k": 20, "forward_s": ms_f * 1e-3,
+    emit({"suite": "mixture_n50000_d32_k20_backward", "n": len(X), "d": 32, "k": 20, "forward_s": ms_f * 1e-3,
           "backward_s": (ms_fb - ms_f) * 1e-3, "forward_backward_s": ms_fb * 1e-3,
           "agreement": {"grad_max_rel_err_vs_fp64_autograd": rel, "float32_result": True}})
-    # config 4: 2,048 problems in one batched call against a loop of single calls
-    batched_case(2048, stream, emit, "config4")
+    # 2,048 problems in one batched call against a loop of single calls
+    batched_case(2048, stream, emit, "batched_2048_problems_d16")
     return 0
 
 
@@ -690,7 +691,7 @@ def run_scaling(args):
 
 
 def run_batched(args):
-    """Config 4's workload alone, with --batched problems (a small count
+    """The batched problem mix alone, with --batched problems (a small count
     keeps an ncu capture of the batched kernel short)."""
     import torch
 

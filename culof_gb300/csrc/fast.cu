@@ -1159,8 +1159,9 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
     // The tensor sweep runs two CTAs per SM. Every split of a row tile starts
     // from the loose seed threshold and pays the candidate surge that follows,
     // so it takes few splits: one from two waves of row tiles up, otherwise
-    // about four CTAs per SM slot pair, at most 3 (measured on 20k-50k point
-    // clusters in 32-128 dimensions: 3.9-9.6 ms against 5.0-11.5 ms with 7).
+    // enough for about 4 x SMs CTAs (two waves at two per SM), at most 3
+    // (measured on 20k-50k point clusters in 32-128 dimensions: 3.9-9.6 ms
+    // against 5.0-11.5 ms with 7).
     int nsplit = 1;
     if (nt > 1) {
         if (wide) {

@@ -88,7 +88,7 @@ def test_autograd_function_end_to_end():
     assert _rel(got, g_ref) < 1e-6
 
 
-def test_backward_config3_scale():
+def test_backward_mixture_n50000_d32():
     # n = 50,000, d = 32, k = 20: the sparse backward against FP64 autograd
     # evaluated by torch on the GPU with the same neighbour slots
     X = synthetic.clusters_with_outliers(50000, 32, seed=60)

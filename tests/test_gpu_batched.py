@@ -112,7 +112,7 @@ def test_batched_validation():
             ctx.lof_batched_device([0, 50, 100], [5, 5], dx.data_ptr(), 65, False, ds.data_ptr())
 
 
-def test_batched_config4_subset_bit_exact():
+def test_batched_problem_mix_subset_bit_exact():
     # 2,048 problems, n log-uniform in [128, 16384], d = 16, k in [10, 40]
     probs, ks = synthetic.batched_problems(2048, 16, seed=0)
     with _culof.Context() as ctx:
