@@ -81,6 +81,7 @@ _SIGS = {
     "culof_lof_batched": ([_I, _P, _P, _P, _I, _I, _P], _I),
     "culof_context_lof_batched": ([_P, _I, _P, _P, _P, _I, _I, _P], _I),
     "culof_context_pair_stats": ([_P, ctypes.POINTER(_D), ctypes.POINTER(_D)], _I),
+    "culof_context_probe_bounded_wait": ([_P, ctypes.c_longlong], _I),
     "culof_compute_scores": ([_P, _P, _P, _I64, _I, _P], _I),
     "culof_context_contamination_offset_device": ([_P, _P, _I64, _D, _P], _I),
     "culof_contamination_offset_noalloc": ([_P, _P, _I64, _D, _P], _I),
@@ -320,6 +321,11 @@ class Context:
         ev, tot = _D(0.0), _D(0.0)
         _check(_lib.culof_context_pair_stats(self._h, ctypes.byref(ev), ctypes.byref(tot)))
         return ev.value, tot.value
+
+    def probe_bounded_wait(self, spin_limit: int = 1 << 14) -> None:
+        """Run a bounded wait that never completes; raises CudaError (the
+        failure path of every kernel wait), the context stays usable."""
+        _check(_lib.culof_context_probe_bounded_wait(self._h, int(spin_limit)))
 
     def set_graphs(self, on: bool) -> None:
         _check(_lib.culof_context_set_graphs(self._h, int(bool(on))))

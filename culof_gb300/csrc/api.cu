@@ -155,6 +155,10 @@ int culof_context_pair_stats(culof_context* ctx, double* evaluated_pairs, double
     return guarded([&] { engine_of(ctx).pair_stats(evaluated_pairs, total_pairs); });
 }
 
+int culof_context_probe_bounded_wait(culof_context* ctx, long long spin_limit) {
+    return guarded([&] { engine_of(ctx).probe_bounded_wait(spin_limit); });
+}
+
 int culof_lof(const float* points, int64_t n_points, int n_dims, int k, int normalize, float* scores_out) {
     return guarded([&] {
         culof_gb300::validate_lof_args(points, n_points, n_dims, k);

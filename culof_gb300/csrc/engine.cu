@@ -11,13 +11,27 @@
 
 #include "engine.cuh"
 #include "fast.cuh"
+#include "sweep_common.cuh"
 #include "tc_host.cuh"
 
 namespace culof_gb300 {
 
 namespace {
 std::atomic<unsigned long long> g_launches{0};
+
+// A wait on an mbarrier phase that nothing completes, bounded like every
+// wait of the engine's kernels: after `limit` polls it gives up, sets the
+// status word and returns, so the context stays usable.
+__global__ void wait_probe_kernel(int* status, long long limit) {
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) {
+        sweep::mbar_init(&bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && !sweep::mbar_wait(&bar, 0, limit)) atomicExch(status, 1);
 }
+}  // namespace
 
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 void count_launches(unsigned long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
@@ -271,6 +285,15 @@ void Engine::pair_stats(double* evaluated, double* total) {
     // one block = 16 rows x 128 columns
     if (evaluated) *evaluated = static_cast<double>(ev) * 16.0 * 128.0;
     if (total) *total = static_cast<double>(stat_total_blocks_) * 16.0 * 128.0;
+}
+
+void Engine::probe_bounded_wait(long long limit) {
+    if (limit < 1 || limit > sweep::kSpinLimit) throw Error(kInvalidArgument, "spin limit out of range");
+    CG_CUDA(cudaSetDevice(device_));
+    CG_CUDA(cudaMemsetAsync(status_ptr(), 0, sizeof(int), stream_));
+    wait_probe_kernel<<<1, 32, 0, stream_>>>(status_ptr(), limit);
+    CG_LAUNCH_CHECK();
+    check_status();
 }
 
 void Engine::check_status() {

@@ -167,6 +167,9 @@ public:
     // Raises kKernelFault if a kernel of the last call reported an error
     // (synchronises the stream).
     void check_status();
+    // Runs a bounded wait that never completes (limit polls) and reports it
+    // like a kernel's expired wait: raises kKernelFault. Test support.
+    void probe_bounded_wait(long long limit);
 
     // Stage timing with CUDA events on the launching stream. Stages:
     // 0 centre+norms, 1 spatial order+tiles, 2 seed, 3 sweep (or the general

@@ -84,8 +84,8 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
     return ok != 0;
 }
 // Bounded wait: false if the phase never completes (the caller reports it).
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
-    for (long long it = 0; it < kSpinLimit; ++it) {
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, long long limit = kSpinLimit) {
+    for (long long it = 0; it < limit; ++it) {
         if (mbar_try_wait(bar, parity)) return true;
         if (it > 64) __nanosleep(64);
     }

@@ -119,6 +119,14 @@ CULOF_API unsigned long long culof_kernel_launch_count(void);
  * other paths. Synchronises the context stream. */
 CULOF_API int culof_context_pair_stats(culof_context* ctx, double* evaluated_pairs, double* total_pairs);
 
+/* Test support for the failure path. Every wait in the library's kernels is
+ * bounded: when it runs out, the kernel sets the context's status word and
+ * returns, and the call fails with CULOF_ERR_KERNEL while the context stays
+ * usable. This runs one such wait on a barrier phase that nothing completes,
+ * giving up after spin_limit polls (1 .. 2^24), so it returns
+ * CULOF_ERR_KERNEL. Synchronises the context stream. */
+CULOF_API int culof_context_probe_bounded_wait(culof_context* ctx, long long spin_limit);
+
 /* Measured FP32 CUDA-core throughput of the current device in TFLOP/s
  * (packed = 1: fma.rn.f32x2; 0: scalar fma.rn.f32), the roofline
  * denominator of the FP32 distance sweep. No reference counterpart. */

@@ -126,3 +126,18 @@ def test_rejects_non_finite_input():
     X[3, 1] = np.nan
     with pytest.raises(ValueError, match="NaN or infinity"):
         lof(X, 10)
+
+
+def test_expired_bounded_wait_reports_an_error_and_the_context_stays_usable():
+    # every wait in the kernels is bounded: when one runs out the kernel sets
+    # a status word and returns, and the call fails instead of hanging
+    from culof_gb300 import _culof
+
+    X = synthetic.clusters_with_outliers(2000, 8, seed=40)
+    with _culof.Context() as ctx:
+        with pytest.raises(_culof.CudaError, match="bounded wait"):
+            ctx.probe_bounded_wait(1 << 12)
+        got = ctx.lof(X, 20)
+        with pytest.raises(ValueError):
+            ctx.probe_bounded_wait(0)
+    np.testing.assert_array_equal(got.view(np.uint32), oracle.lof(X, 20).view(np.uint32))
