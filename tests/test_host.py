@@ -115,3 +115,44 @@ def test_no_device_raises_cuda_error(gpu_available):
     assert issubclass(culof_gb300.CudaError, RuntimeError)
     with pytest.raises(culof_gb300.CudaError):
         _culof.Context()
+
+
+CXX_CALLER = r"""
+#include <culof.h>
+#include <cstdio>
+#include <stdexcept>
+#include <vector>
+int main() {
+    std::vector<float> x(200 * 4);
+    for (size_t i = 0; i < x.size(); ++i) x[i] = static_cast<float>((i * 37) % 101) * 0.01f;
+    try {
+        culof::lof(nullptr, 200, 4, 20);
+    } catch (const std::invalid_argument& e) {
+        std::printf("invalid_argument: %s\n", e.what());
+    }
+    try {
+        std::printf("scores: %zu\n", culof::lof(x.data(), 200, 4, 20).size());
+    } catch (const culof::CudaError& e) {
+        std::printf("CudaError: %s\n", e.what());
+    }
+    return 0;
+}
+"""
+
+
+def test_cxx_caller_relinks_unchanged(tmp_path, gpu_available):
+    # a program written against the reference's culof.h builds and links
+    # against this library, with the reference's exceptions and messages
+    src = tmp_path / "app.cpp"
+    src.write_text(CXX_CALLER)
+    exe = tmp_path / "app"
+    libdir = os.path.dirname(_culof.LIB_PATH)
+    try:
+        build = subprocess.run(["g++", str(src), "-I", os.path.join(ROOT, "include"), "-L", libdir, "-lculof_gb300",
+                                f"-Wl,-rpath,{libdir}", "-o", str(exe)], capture_output=True, text=True)
+    except FileNotFoundError:
+        pytest.skip("g++ unavailable")
+    assert build.returncode == 0, build.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120).stdout
+    assert "invalid_argument: points must not be null" in out
+    assert ("scores: 200" if gpu_available else "CudaError: no CUDA device available") in out
