@@ -125,15 +125,18 @@ def test_knn_without_prune_lists_bit_exact(ctx, monkeypatch, name):
 
 
 def test_auto_selects_the_fast_path_for_small_d(ctx):
-    X = synthetic.clusters_with_outliers(3000, 8, seed=1)
+    X = synthetic.clusters_with_outliers(6000, 8, seed=1)
     ctx.lof(X, 20)
     assert ctx.last_path() == _culof.PATH_FAST
+    # up to 4096 points the general path's few kernels beat the fused paths
+    ctx.lof(synthetic.clusters_with_outliers(3000, 8, seed=1), 20)
+    assert ctx.last_path() == _culof.PATH_GENERAL
     ctx.lof(synthetic.reference_test_data(600, 4, seed=5), 257)
     assert ctx.last_path() == _culof.PATH_GENERAL
-    ctx.lof(synthetic.reference_test_data(600, 32, seed=5), 20)
+    ctx.lof(synthetic.reference_test_data(6000, 32, seed=5), 20)
     assert ctx.last_path() == _culof.PATH_TENSOR
     # 8 < d <= 16: the FP32 wide sweep below one wave of tensor CTAs, else the tensor path
-    ctx.lof(synthetic.reference_test_data(600, 12, seed=5), 20)
+    ctx.lof(synthetic.reference_test_data(6000, 12, seed=5), 20)
     assert ctx.last_path() == _culof.PATH_FAST
     ctx.lof(synthetic.clusters_with_outliers(40_000, 16, seed=5), 20)
     assert ctx.last_path() == _culof.PATH_TENSOR
