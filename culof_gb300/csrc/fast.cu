@@ -8,8 +8,10 @@
 //  1. spatial order: a 32-bit Morton key of the centred coordinates, sorted
 //     with a stable LSD radix sort; tiles of 128 consecutive sorted points
 //     are spatially compact.
-//  2. seed: per row, the exact k best over its own tile (warp bitonic sort of
-//     128 exact keys). Its k-th key K bounds the row's true k-th key.
+//  2. seed: per row, the exact k best over its own tile and the four nearest
+//     tiles in Morton order (T+-1, T+-2), by warp bitonic sorts and merges.
+//     Its k-th key K bounds the row's true k-th key; the sweep covers every
+//     later tile.
 //  3. sweep: each CTA owns 128 rows and streams column tiles (TMA bulk
 //     copies into shared memory, nearest tiles first); each warp owns 16 of
 //     the rows (4 per lane, in registers as -2a). For every pair it
