@@ -20,13 +20,16 @@ offset and the labels.
   farther than every k-th neighbour; the pairs it actually evaluated, the
   pruned fraction and its FLOP rate on the evaluated pairs are reported
   beside it (executed_tflops, executed_frac).
-* cpu_baseline: the CPU oracle (a C restatement of the same exact algorithm,
-  all host threads) on a bounded sample of rows of the same workload.
+* cpu_baseline: one whole fit_predict of the same workload (centre, exact
+  k-NN of all n rows, LRD, scores, offset, labels) by the CPU oracle, a C
+  restatement of the same exact algorithm, on all host threads.
 
 ``--impl reference`` times the reference's CPU implementation of this path
-instead: the reference's own CPU comparison path (scikit-learn) is not on the
-GPU host and its CUDA build does not run there, so the CPU port of its
-algorithm (oracle/) stands in, on all host threads, over a bounded sample.
+instead: whole fit_predict steps of the CPU port of its algorithm (oracle/),
+on all host threads, the mean of the timed steps. The reference's own CPU
+comparison path (scikit-learn) is not on the GPU host and its CUDA build does
+not run there. That arm never loads the engine's library: the workload
+generator is loaded by path.
 
 Under torchrun with N > 1 every rank runs an independent replica on its own
 GPU (no collective on the data path); value sums the ranks' work over the
@@ -84,7 +87,6 @@ def parse_args():
     p.add_argument("--k", type=int, default=20)
     p.add_argument("--contamination", type=float, default=0.01)
     p.add_argument("--seed", type=int, default=1)
-    p.add_argument("--cpu-seconds", type=float, default=8.0, help="target CPU time of the baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--path", choices=["auto", "fast", "general", "tensor"], default="auto")
     p.add_argument("--suite", action="store_true",
@@ -107,9 +109,20 @@ def dist_env():
     return world, rank, local
 
 
-def workload(args):
-    from culof_gb300 import synthetic
+def load_synthetic():
+    """culof_gb300/synthetic.py by path (numpy only): importing the package
+    would load the engine's library, which the CPU arm must not touch."""
+    import importlib.util
 
+    spec = importlib.util.spec_from_file_location("culof_gb300_synthetic",
+                                                  os.path.join(ROOT, "culof_gb300", "synthetic.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def workload(args):
+    synthetic = load_synthetic()
     if args.workload == "factor":
         return synthetic.factor_model(args.n, args.d, seed=args.seed)
     if args.workload == "mixture":
@@ -220,39 +233,31 @@ class ClockSampler:
 # ----------------------------------------------------------------- CPU legs
 
 
-def cpu_sample(args, X, target_s: float):
-    """Oracle exact k-NN (the dominant cost of the CPU path) over a bounded
-    sample of rows on all host threads; returns (pair-dists/s, rows, seconds)."""
+def cpu_fit_predict_s(args, X) -> float:
+    """Wall time of one whole fit_predict by the CPU oracle on all host threads."""
     import oracle
 
     oracle.build()
-    Xc, _, _ = oracle.center(X)
-    n = X.shape[0]
-    rows = 64
     t0 = time.perf_counter()
-    oracle.knn(Xc, args.k, rows=(0, rows))
-    dt = time.perf_counter() - t0
-    rows = int(min(n, max(rows, rows * target_s / max(dt, 1e-6))))
-    t0 = time.perf_counter()
-    oracle.knn(Xc, args.k, rows=(0, rows))
-    dt = time.perf_counter() - t0
-    return rows * float(n) / dt, rows, dt
+    oracle.fit_predict(X, args.k, args.contamination)
+    return time.perf_counter() - t0
 
 
 def run_reference(args):
     world, rank, _ = dist_env()
     if rank != 0:
         return 0
+    import oracle
+
+    oracle.build()
     X = workload(args)
     n = X.shape[0]
     cores = os.cpu_count() or 1
-    target = max(1.0, min(args.cpu_seconds, 120.0 / max(1, args.steps + args.warmup)))
-    vals, rows_used = [], 0
-    for i in range(args.warmup + args.steps):
-        v, rows_used, dt = cpu_sample(args, X, target)
-        if i >= args.warmup:
-            vals.append(v)
-    value = statistics.mean(vals)
+    for _ in range(args.warmup):
+        cpu_fit_predict_s(args, X)
+    step_s = [cpu_fit_predict_s(args, X) for _ in range(args.steps)]
+    mean_s = statistics.mean(step_s)
+    value = float(n) * n / mean_s
     line = {
         "impl": "reference",
         "metric": "pair-dists/s",
@@ -261,21 +266,23 @@ def run_reference(args):
         "n_gpus": args.gpus,
         "steps": args.steps,
         "warmup": args.warmup,
-        "ms_per_step": float(n) * n / value * 1e3,
+        "ms_per_step": mean_s * 1e3,
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic",
         "config": config_dict(args),
+        "fit_predict_s": mean_s,
         "cpu_baseline": {
             "value": value,
             "unit": "pair-dists/s",
             "cores": cores,
             "kind": "port",
-            "sample": f"exact k-NN of {rows_used} rows against all {n} points per step (C port of the reference "
-            f"algorithm, {cores} threads); the reference's CPU comparison path (scikit-learn) is not installed on "
-            "the GPU host and its CUDA build cannot run there",
+            "sample": f"every step one whole fit_predict of all {n} rows (centre, exact k-NN, LRD, scores, offset, "
+            f"labels) by the C port of the reference algorithm on {cores} threads; mean of {args.steps} timed "
+            "steps. The reference's CPU comparison path (scikit-learn) is not installed on the GPU host and its "
+            "CUDA build cannot run there",
         },
         "e2e": {"value": value, "unit": "pair-dists/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -447,13 +454,13 @@ def run_ours(args):
         }
     cpu = None
     if not args.no_cpu_baseline:
-        v, rows, dt = cpu_sample(args, X, args.cpu_seconds)
+        dt = cpu_fit_predict_s(args, X)
         cpu = {
-            "value": v,
+            "value": pairs / dt,
             "unit": "pair-dists/s",
             "cores": os.cpu_count() or 1,
             "kind": "port",
-            "sample": f"exact k-NN of {rows} rows against all {n} points ({dt:.1f} s), C port of the same algorithm",
+            "sample": f"one whole fit_predict of all {n} rows ({dt:.2f} s): the C port of the same algorithm",
         }
     value = world * pairs / (mean_ms * 1e-3)
     line = {
@@ -469,7 +476,8 @@ def run_ours(args):
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic",
-        "config": config_dict(args, {"path": PATH_NAMES[ctx.last_path()]}),
+        "config": config_dict(args),
+        "path": PATH_NAMES[ctx.last_path()],
         "fit_predict_s": mean_ms * 1e-3,
         "e2e": {
             "value": world * pairs / (e2e_mean * 1e-3),
@@ -512,7 +520,7 @@ def _time_calls(fn, stream, warm=2, reps=5):
     return e0.elapsed_time(e1) / reps
 
 
-def batched_case(count, stream, emit, label):
+def batched_case(count, stream, emit, label, fp64=False):
     """The batched problem mix with `count` problems: one batched call (CUDA
     graph replay after the first call) against a loop of single calls, and
     the scores of both compared bit for bit."""
@@ -541,12 +549,26 @@ def batched_case(count, stream, emit, label):
             ctx.lof_device(dps[i].data_ptr(), len(probs[i]), 16, ks[i], False, outs[offs[i]:offs[i + 1]].data_ptr())
 
     ms_l = _time_calls(loop, stream, warm=1, reps=2)
-    same = bool(np.array_equal(ds.cpu().numpy().view(np.uint32), outs.cpu().numpy().view(np.uint32)))
-    emit({"suite": label, "problems": len(probs), "points": int(offs[-1]), "d": 16,
-          "pairs": float(sum(float(len(p)) ** 2 for p in probs)),
-          "batched_s": ms_b * 1e-3, "loop_of_single_calls_s": ms_l * 1e-3, "speedup_vs_loop": ms_l / ms_b,
-          "first_call_s_plan_autotune_capture": first_s,
-          "agreement": {"bit_exact_vs_single_calls": same}})
+    scores = ds.cpu().numpy()
+    same = bool(np.array_equal(scores.view(np.uint32), outs.cpu().numpy().view(np.uint32)))
+    line = {"suite": label, "problems": len(probs), "points": int(offs[-1]), "d": 16,
+            "pairs": float(sum(float(len(p)) ** 2 for p in probs)),
+            "batched_s": ms_b * 1e-3, "loop_of_single_calls_s": ms_l * 1e-3, "speedup_vs_loop": ms_l / ms_b,
+            "first_call_s_plan_autotune_capture": first_s,
+            "agreement": {"bit_exact_vs_single_calls": same}}
+    if fp64:
+        import oracle
+
+        # FP64 error over a seeded sample of up to 64 problems
+        pick = np.sort(np.random.default_rng(64).choice(len(probs), min(64, len(probs)), replace=False))
+        rel = []
+        for i in pick:
+            ref = oracle.lof_f64(probs[i], ks[i])
+            rel.append(np.abs(scores[offs[i]:offs[i + 1]].astype(np.float64) - ref) / ref)
+        rel = np.concatenate(rel)
+        line["fp64_err"] = {"median": float(np.median(rel)), "p99": float(np.quantile(rel, 0.99)),
+                            "max": float(rel.max()), "over": f"every score of {len(pick)} seeded problems"}
+    emit(line)
     ctx.close()
 
 
@@ -601,18 +623,26 @@ def run_suite(args):
         ctx.close()
         return res, nof.cpu().numpy()
 
-    # clusters, d = 8, k = 20, c = 0.01, at n = 20k and 200k
+    # clusters, d = 8, k = 20, c = 0.01, at n = 20k and 200k; the scores'
+    # relative error against the FP64 brute force of all n points
     for name, n in (("clusters_n20000_d8_k20", 20_000), ("clusters_n200000_d8_k20", 200_000)):
         X = synthetic.clusters_with_outliers(n, 8, seed=1)
-        res, _ = fit_predict_case(name, X, 20, 0.01, 0, 2000)
+        res, nof = fit_predict_case(name, X, 20, 0.01, 0, 2000)
+        res["fp64_err"] = dict(oracle.fp64_error(-nof, X, 20), over=f"all {n} scores")
         emit(res)
-    # factor model, n = 200k, d = 128, k = 50: tensor path against the FP32 sweep
+    # factor model, n = 200k, d = 128, k = 50: tensor path against the FP32
+    # sweep; FP64 error of the LOF of a seeded 5,000-row subsample
     X = synthetic.factor_model(200_000, 128, seed=1)
     tres, tnof = fit_predict_case("factor_n200000_d128_k50", X, 50, 0.01, 3, 500)
     fres, fnof = fit_predict_case("factor_n200000_d128_k50_fp32", X, 50, 0.01, 1, 1)
     tres["fp32_fit_predict_s"] = fres["fit_predict_s"]
     tres["speedup_vs_fp32"] = fres["fit_predict_s"] / tres["fit_predict_s"]
     tres["agreement"]["nof_bit_exact_vs_fp32_path"] = bool(np.array_equal(tnof.view(np.uint32), fnof.view(np.uint32)))
+    Xs = np.ascontiguousarray(X[np.sort(np.random.default_rng(5000).choice(len(X), 5000, replace=False))])
+    with _culof.Context() as ctx:
+        ctx.set_path(_culof.PATH_TENSOR)
+        s_sub = ctx.lof(Xs, 50)
+    tres["fp64_err"] = dict(oracle.fp64_error(s_sub, Xs, 50), over="LOF of a seeded 5,000-row subsample")
     emit(tres)
     # sparse backward, mixture, n = 50,000, d = 32, k = 20
     from culof_gb300.autograd import lof_scores
@@ -638,11 +668,13 @@ def run_suite(args):
     X64 = Xt.double().requires_grad_(True)
     (ob.lof_fixed(X64, idx.long(), False) * w).sum().backward()
     rel = float((g - X64.grad).abs().max() / X64.grad.abs().max())
+    fwd = lof_scores(Xt, 20).cpu().numpy()
     emit({"suite": "mixture_n50000_d32_k20_backward", "n": len(X), "d": 32, "k": 20, "forward_s": ms_f * 1e-3,
           "backward_s": (ms_fb - ms_f) * 1e-3, "forward_backward_s": ms_fb * 1e-3,
-          "agreement": {"grad_max_rel_err_vs_fp64_autograd": rel, "float32_result": True}})
+          "agreement": {"grad_max_rel_err_vs_fp64_autograd": rel, "float32_result": True},
+          "fp64_err": dict(oracle.fp64_error(fwd, X, 20), over="all 50000 forward scores")})
     # 2,048 problems in one batched call against a loop of single calls
-    batched_case(2048, stream, emit, "batched_2048_problems_d16")
+    batched_case(2048, stream, emit, "batched_2048_problems_d16", fp64=True)
     return 0
 
 

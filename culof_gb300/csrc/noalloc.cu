@@ -13,10 +13,16 @@
 //
 // Set-up: the first call on a device looks up the array's device address
 // with cudaGetSymbolAddress (with that device current) and caches it, so
-// make that first call before any stream capture.
+// make that first call before any stream capture. The cache is keyed on the
+// current CUDA context's unique id: a context that the caller's framework
+// destroys and creates again (cudaDeviceReset) gets a fresh lookup on its
+// first call, never the old context's address.
+// The stream must belong to the current device.
 // Sharing: every call on a device uses the same array, which keeps the last
 // call's contents; each call clears the histogram and state first. Calls that
 // overlap on the GPU (e.g. on two streams at once) race on the array.
+#include <cuda.h>
+
 #include <mutex>
 #include <sstream>
 #include <string>
@@ -41,25 +47,62 @@ constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) unsigned char g_offset_scratch[kNoAllocScratchBytes];
 
-std::mutex g_setup_mutex;
-void* g_scratch_addr[kMaxDevices] = {};
+struct ScratchSlot {
+    void* addr = nullptr;
+    unsigned long long context_id = 0;
+};
 
-// Device address of g_offset_scratch on the current device (set up once per
-// device). In host code the array's name is only a host-side stand-in.
+std::mutex g_setup_mutex;
+ScratchSlot g_scratch[kMaxDevices];
+
+// Unique id of the calling thread's current CUDA context (0: none current, or
+// the driver cannot say). The driver functions come through the runtime's
+// entry-point query, so the library needs no link to the driver library.
+unsigned long long current_context_id() {
+    using GetCurrentFn = CUresult (*)(CUcontext*);
+    using GetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+    static GetCurrentFn get_current = nullptr;
+    static GetIdFn get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<GetCurrentFn>(f);
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<GetIdFn>(f);
+    });
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (!get_current || !get_id || get_current(&ctx) != CUDA_SUCCESS || ctx == nullptr) return 0;
+    if (get_id(ctx, &id) != CUDA_SUCCESS) return 0;
+    return id;
+}
+
+// Device address of g_offset_scratch in the current device's context, looked
+// up once per (device, context). In host code the array's name is only a
+// host-side stand-in, never a device address.
 void* scratch_address() {
     int dev = 0;
     CG_CUDA(cudaGetDevice(&dev));
     if (dev < 0 || dev >= kMaxDevices) throw Error(kInternal, "device ordinal out of range");
     std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (g_scratch_addr[dev] == nullptr) {
+    ScratchSlot& slot = g_scratch[dev];
+    const unsigned long long ctx = current_context_id();
+    if (slot.addr == nullptr || ctx == 0 || slot.context_id != ctx) {
         void* p = nullptr;
         const cudaError_t e = cudaGetSymbolAddress(&p, g_offset_scratch);
         if (e != cudaSuccess)
             throw Error(kCudaError, std::string("cudaGetSymbolAddress(offset scratch) failed: ") +
                                         cudaGetErrorString(e));
-        g_scratch_addr[dev] = p;
+        slot.addr = p;
+        // the lookup makes the device's context current if none was
+        slot.context_id = current_context_id();
     }
-    return g_scratch_addr[dev];
+    return slot.addr;
 }
 
 }  // namespace

@@ -227,9 +227,12 @@ CULOF_API int culof_context_contamination_offset_device(culof_context* ctx, cons
  * that loads the library holds until the process exits. n_points must be at
  * most 2^31 - 1 (larger sizes are rejected with CULOF_ERR_INVALID_ARGUMENT).
  * The first call on a device looks up the array's address (cudaGetSymbolAddress);
- * make it before any stream capture. Every call shares the array and clears
- * it first; calls that overlap on the GPU race on it. Asynchronous on
- * cuda_stream. It has no counterpart in the reference. */
+ * make it before any stream capture. The address is cached per device and
+ * CUDA context, so a re-created context (cudaDeviceReset) gets its own
+ * lookup on its first call. Every call shares the array and clears it first;
+ * calls that overlap on the GPU race on it. Asynchronous on cuda_stream,
+ * which must belong to the current device. It has no counterpart in the
+ * reference. */
 CULOF_API int culof_contamination_offset_noalloc(void* cuda_stream, const float* d_nof, int64_t n_points,
                                                  double contamination, double* d_offset);
 

@@ -69,6 +69,10 @@ def _load():
             lib.oracle_percentile_offset.restype = dbl
             lib.oracle_labels.argtypes = [P, i64, dbl, P]
             lib.oracle_ref_select_tile.argtypes = [P, P, i32, i64, i64, i32, P, P, P]
+            lib.oracle_knn_list.argtypes = [P, i64, i32, i32, P, i64, P, P, P, i32]
+            lib.oracle_knn_f64.argtypes = [P, i64, i32, i32, i32, P, i64, P, P, i32]
+            lib.oracle_lof_f64.argtypes = [P, i64, i32, i32, i32, P, i32]
+            lib.oracle_lof_f64.restype = i32
             _lib = lib
     return _lib
 
@@ -180,3 +184,52 @@ def ref_select_tile(tile, norms_, row_offset: int, k: int):
         _ptr(tile), _ptr(_f32(norms_)), rows, row_offset, n, k, _ptr(idx), _ptr(d2), _ptr(kd)
     )
     return idx, d2, kd
+
+
+def knn_list(Xc, k: int, rows, nthreads: int = 0):
+    """Exact k-NN (the same select as ``knn``) of the listed rows over all of
+    Xc: (nbr_idx int32 (k, m), nbr_d2 float32 (k, m), kdist2 float32 (m,)),
+    column r for row ``rows[r]``."""
+    Xc = _f32(Xc)
+    n, d = Xc.shape
+    rows = np.ascontiguousarray(rows, np.int64)
+    m = rows.shape[0]
+    idx = np.empty((k, m), np.int32)
+    d2 = np.empty((k, m), np.float32)
+    kd = np.empty(m, np.float32)
+    _load().oracle_knn_list(_ptr(Xc), n, d, k, _ptr(rows), m, _ptr(idx), _ptr(d2), _ptr(kd), nthreads)
+    return idx, d2, kd
+
+
+def knn_f64(X, kk: int, normalize: bool = False, rows=None, nthreads: int = 0):
+    """FP64 brute-force neighbours of the listed rows (default all): the kk
+    nearest by (Euclidean distance, index), as (idx int64 (m, kk), dist
+    float64 (m, kk)), ascending. Centres (and z-scores) in double first."""
+    X = _f32(X)
+    n, d = X.shape
+    lst = None if rows is None else np.ascontiguousarray(rows, np.int64)
+    m = n if lst is None else lst.shape[0]
+    idx = np.empty((m, kk), np.int64)
+    dist = np.empty((m, kk), np.float64)
+    _load().oracle_knn_f64(_ptr(X), n, d, int(normalize), kk, None if lst is None else _ptr(lst), m,
+                           _ptr(idx), _ptr(dist), nthreads)
+    return idx, dist
+
+
+def lof_f64(X, k: int = 20, normalize: bool = False, nthreads: int = 0) -> np.ndarray:
+    """FP64 brute-force LOF scores from the definitions (the yardstick of the
+    float32 engine's error; not bit-exact with it)."""
+    X = _f32(X)
+    n, d = X.shape
+    out = np.empty(n, np.float64)
+    if _load().oracle_lof_f64(_ptr(X), n, d, k, int(normalize), _ptr(out), nthreads) != 0:
+        raise ValueError("oracle_lof_f64: invalid arguments")
+    return out
+
+
+def fp64_error(scores, X, k: int, normalize: bool = False) -> dict:
+    """Median, p99 and max relative error of float32 LOF scores against the
+    FP64 brute force of the same points."""
+    ref = lof_f64(X, k, normalize)
+    rel = np.abs(np.asarray(scores, np.float64) - ref) / np.maximum(np.abs(ref), 1e-300)
+    return {"median": float(np.median(rel)), "p99": float(np.quantile(rel, 0.99)), "max": float(rel.max())}

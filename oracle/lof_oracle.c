@@ -173,7 +173,8 @@ typedef struct {
     float* kdist2;
 } knn_job;
 
-static void knn_one_row(const knn_job* J, int64_t i, uint64_t* heap, float* dbuf) {
+/* The k smallest keys of row i against every column (unordered, in heap). */
+static void select_row(const knn_job* J, int64_t i, uint64_t* heap, float* dbuf) {
     const int64_t n = J->n;
     const int d = J->d, k = J->k;
     const float* a = J->xc + i * d;
@@ -195,13 +196,28 @@ static void knn_one_row(const knn_job* J, int64_t i, uint64_t* heap, float* dbuf
             }
         }
     }
-    emit_row(heap, k, n, i, J->nbr_idx, J->nbr_d2, J->kdist2);
+}
+
+static void knn_one_row(const knn_job* J, int64_t i, uint64_t* heap, float* dbuf) {
+    select_row(J, i, heap, dbuf);
+    emit_row(heap, J->k, J->n, i, J->nbr_idx, J->nbr_d2, J->kdist2);
 }
 
 typedef struct {
     const knn_job* job;
     int64_t begin, end;
 } knn_slice;
+
+/* Feature-major copy of the points per block of KNN_BLK columns, zero padded. */
+static float* column_blocks(const float* xc, int64_t n, int d) {
+    const int64_t nblk = (n + KNN_BLK - 1) / KNN_BLK;
+    float* colT = (float*)calloc((size_t)(nblk * KNN_BLK) * (size_t)d, sizeof(float));
+    for (int64_t j = 0; j < n; ++j) {
+        const int64_t b = j / KNN_BLK, jj = j % KNN_BLK;
+        for (int f = 0; f < d; ++f) colT[b * KNN_BLK * d + (int64_t)f * KNN_BLK + jj] = xc[j * d + f];
+    }
+    return colT;
+}
 
 static void* knn_worker(void* p) {
     const knn_slice* s = (const knn_slice*)p;
@@ -216,13 +232,7 @@ static void* knn_worker(void* p) {
 void oracle_knn_rows(const float* xc, int64_t n, int d, int k, int64_t row_begin,
                      int64_t row_end, int32_t* nbr_idx, float* nbr_d2, float* kdist2,
                      int nthreads) {
-    /* Feature-major copy per block of KNN_BLK columns, zero padded. */
-    const int64_t nblk = (n + KNN_BLK - 1) / KNN_BLK;
-    float* colT = (float*)calloc((size_t)(nblk * KNN_BLK) * (size_t)d, sizeof(float));
-    for (int64_t j = 0; j < n; ++j) {
-        const int64_t b = j / KNN_BLK, jj = j % KNN_BLK;
-        for (int f = 0; f < d; ++f) colT[b * KNN_BLK * d + (int64_t)f * KNN_BLK + jj] = xc[j * d + f];
-    }
+    float* colT = column_blocks(xc, n, d);
     knn_job job = {xc, colT, n, d, k, row_begin, row_end, nbr_idx, nbr_d2, kdist2};
     int nt = resolve_threads(nthreads);
     const int64_t rows = row_end - row_begin;
@@ -362,4 +372,228 @@ void oracle_ref_select_tile(const float* tile, const float* norms, int rows,
         emit_row(heap, k, n, self, nbr_idx, nbr_d2, kdist2);
     }
     free(heap);
+}
+
+/* ------------------------------------------------ k-NN of a list of rows */
+
+typedef struct {
+    const knn_job* job;
+    const int64_t* rows;
+    int64_t m, begin, end;
+} list_slice;
+
+/* Row rows[r] goes to column r of the (k x m) outputs: emit_row with a
+ * row count of m and point index r. */
+static void* knn_list_worker(void* p) {
+    const list_slice* s = (const list_slice*)p;
+    const knn_job* J = s->job;
+    uint64_t* heap = (uint64_t*)malloc(sizeof(uint64_t) * (size_t)J->k);
+    float* dbuf = (float*)malloc(sizeof(float) * KNN_BLK);
+    for (int64_t r = s->begin; r < s->end; ++r) {
+        select_row(J, s->rows[r], heap, dbuf);
+        emit_row(heap, J->k, s->m, r, J->nbr_idx, J->nbr_d2, J->kdist2);
+    }
+    free(heap);
+    free(dbuf);
+    return NULL;
+}
+
+void oracle_knn_list(const float* xc, int64_t n, int d, int k, const int64_t* rows, int64_t m,
+                     int32_t* nbr_idx, float* nbr_d2, float* kdist2, int nthreads) {
+    float* colT = column_blocks(xc, n, d);
+    knn_job job = {xc, colT, n, d, k, 0, n, nbr_idx, nbr_d2, kdist2};
+    int nt = resolve_threads(nthreads);
+    if (nt > m) nt = m > 0 ? (int)m : 1;
+    pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * (size_t)nt);
+    list_slice* sl = (list_slice*)malloc(sizeof(list_slice) * (size_t)nt);
+    for (int t = 0; t < nt; ++t) {
+        sl[t].job = &job;
+        sl[t].rows = rows;
+        sl[t].m = m;
+        sl[t].begin = m * t / nt;
+        sl[t].end = m * (t + 1) / nt;
+        pthread_create(&th[t], NULL, knn_list_worker, &sl[t]);
+    }
+    for (int t = 0; t < nt; ++t) pthread_join(th[t], NULL);
+    free(th);
+    free(sl);
+    free(colT);
+}
+
+/* ------------------------------------------------- FP64 brute force LOF */
+
+/* The LOF definitions (Breunig et al. 2000) evaluated in double precision,
+ * as the reference's own test oracle cpu_lof does (tests/cpp/test_culof.cu:
+ * 39-80): centring in double (x - mean, divided by the population standard
+ * deviation for normalize, a zero-variance feature keeping scale 1 as
+ * preprocess.cu:62-65 does), Euclidean distances in double by direct
+ * differences, neighbours = the k smallest (distance, index) pairs other
+ * than the point itself, k-distance = distance to the k-th of them,
+ * reach = max(k-distance(o), d(p, o)), lrd = 1 / (mean reach + 1e-10),
+ * LOF = mean lrd(o) / lrd(p). This is the FP64 yardstick of the float32
+ * engine's error, not a bit-exact restatement. */
+
+typedef struct {
+    double d2;
+    int64_t j;
+} pair64;
+
+static int pair_less(pair64 a, pair64 b) { return a.d2 < b.d2 || (a.d2 == b.d2 && a.j < b.j); }
+
+static void heap64_sift_down(pair64* h, int k, int i) {
+    for (;;) {
+        int l = 2 * i + 1, r = l + 1, m = i;
+        if (l < k && pair_less(h[m], h[l])) m = l;
+        if (r < k && pair_less(h[m], h[r])) m = r;
+        if (m == i) return;
+        pair64 t = h[i];
+        h[i] = h[m];
+        h[m] = t;
+        i = m;
+    }
+}
+
+static int cmp_pair64(const void* a, const void* b) {
+    const pair64 x = *(const pair64*)a, y = *(const pair64*)b;
+    return pair_less(x, y) ? -1 : (pair_less(y, x) ? 1 : 0);
+}
+
+static double* center_f64(const float* x, int64_t n, int d, int normalize) {
+    double* xc = (double*)malloc(sizeof(double) * (size_t)n * (size_t)d);
+    for (int f = 0; f < d; ++f) {
+        double s = 0.0;
+        for (int64_t i = 0; i < n; ++i) s += (double)x[i * d + f];
+        const double mean = s / (double)n;
+        double inv = 1.0;
+        if (normalize) {
+            double v = 0.0;
+            for (int64_t i = 0; i < n; ++i) {
+                const double t = (double)x[i * d + f] - mean;
+                v += t * t;
+            }
+            const double sd = sqrt(v / (double)n);
+            inv = (sd > 1e-12) ? 1.0 / sd : 1.0;
+        }
+        for (int64_t i = 0; i < n; ++i) xc[i * d + f] = ((double)x[i * d + f] - mean) * inv;
+    }
+    return xc;
+}
+
+#define F64_BLK 128
+
+typedef struct {
+    const double* xc;
+    const double* colT; /* feature-major per block of F64_BLK columns */
+    int64_t n;
+    int d, kk;
+    const int64_t* rows; /* output row r is point rows[r] (NULL: point r) */
+    int64_t begin, end;  /* output rows of this worker */
+    int64_t* idx;
+    double* dist;
+} f64_job;
+
+static void* knn_f64_worker(void* p) {
+    const f64_job* J = (const f64_job*)p;
+    const int64_t n = J->n;
+    const int d = J->d, kk = J->kk;
+    pair64* heap = (pair64*)malloc(sizeof(pair64) * (size_t)kk);
+    double dbuf[F64_BLK];
+    for (int64_t r = J->begin; r < J->end; ++r) {
+        const int64_t i = J->rows ? J->rows[r] : r;
+        const double* a = J->xc + i * d;
+        int filled = 0;
+        for (int64_t c0 = 0; c0 < n; c0 += F64_BLK) {
+            const int blk = (n - c0) < F64_BLK ? (int)(n - c0) : F64_BLK;
+            const double* cb = J->colT + c0 * d;
+            for (int jj = 0; jj < F64_BLK; ++jj) dbuf[jj] = 0.0;
+            for (int f = 0; f < d; ++f) {
+                const double af = a[f];
+                const double* c = cb + (size_t)f * F64_BLK;
+                for (int jj = 0; jj < F64_BLK; ++jj) {
+                    const double t = af - c[jj];
+                    dbuf[jj] += t * t;
+                }
+            }
+            for (int jj = 0; jj < blk; ++jj) {
+                const int64_t j = c0 + jj;
+                if (j == i) continue;
+                const pair64 e = {dbuf[jj], j};
+                if (filled < kk) {
+                    heap[filled++] = e;
+                    if (filled == kk)
+                        for (int h = kk / 2 - 1; h >= 0; --h) heap64_sift_down(heap, kk, h);
+                } else if (pair_less(e, heap[0])) {
+                    heap[0] = e;
+                    heap64_sift_down(heap, kk, 0);
+                }
+            }
+        }
+        qsort(heap, (size_t)kk, sizeof(pair64), cmp_pair64);
+        for (int t = 0; t < kk; ++t) {
+            J->idx[r * kk + t] = heap[t].j;
+            J->dist[r * kk + t] = sqrt(heap[t].d2);
+        }
+    }
+    free(heap);
+    return NULL;
+}
+
+static void knn_f64_rows(const double* xc, int64_t n, int d, int kk, const int64_t* row_list, int64_t m,
+                         int64_t* idx, double* dist, int nthreads) {
+    const int64_t nblk = (n + F64_BLK - 1) / F64_BLK;
+    double* colT = (double*)calloc((size_t)(nblk * F64_BLK) * (size_t)d, sizeof(double));
+    /* zero-padded columns beyond n are skipped by the blk bound */
+    for (int64_t j = 0; j < n; ++j) {
+        const int64_t b = j / F64_BLK, jj = j % F64_BLK;
+        for (int f = 0; f < d; ++f) colT[b * F64_BLK * d + (int64_t)f * F64_BLK + jj] = xc[j * d + f];
+    }
+    int nt = resolve_threads(nthreads);
+    if (nt > m) nt = m > 0 ? (int)m : 1;
+    pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * (size_t)nt);
+    f64_job* jobs = (f64_job*)malloc(sizeof(f64_job) * (size_t)nt);
+    for (int t = 0; t < nt; ++t) {
+        f64_job J = {xc, colT, n, d, kk, row_list, m * t / nt, m * (t + 1) / nt, idx, dist};
+        jobs[t] = J;
+        pthread_create(&th[t], NULL, knn_f64_worker, &jobs[t]);
+    }
+    for (int t = 0; t < nt; ++t) pthread_join(th[t], NULL);
+    free(th);
+    free(jobs);
+    free(colT);
+}
+
+void oracle_knn_f64(const float* x, int64_t n, int d, int normalize, int kk, const int64_t* rows,
+                    int64_t m, int64_t* idx, double* dist, int nthreads) {
+    double* xc = center_f64(x, n, d, normalize);
+    knn_f64_rows(xc, n, d, kk, rows, rows ? m : n, idx, dist, nthreads);
+    free(xc);
+}
+
+int oracle_lof_f64(const float* x, int64_t n, int d, int k, int normalize, double* scores, int nthreads) {
+    if (!x || n < 2 || d < 1 || k < 1 || (int64_t)k >= n) return -1;
+    double* xc = center_f64(x, n, d, normalize);
+    int64_t* idx = (int64_t*)malloc(sizeof(int64_t) * (size_t)n * (size_t)k);
+    double* dist = (double*)malloc(sizeof(double) * (size_t)n * (size_t)k);
+    double* lrd = (double*)malloc(sizeof(double) * (size_t)n);
+    knn_f64_rows(xc, n, d, k, NULL, n, idx, dist, nthreads);
+    for (int64_t i = 0; i < n; ++i) {
+        double s = 0.0;
+        for (int t = 0; t < k; ++t) {
+            const int64_t j = idx[i * k + t];
+            const double kd = dist[j * k + k - 1];
+            const double dij = dist[i * k + t];
+            s += kd > dij ? kd : dij;
+        }
+        lrd[i] = 1.0 / (s / (double)k + 1e-10);
+    }
+    for (int64_t i = 0; i < n; ++i) {
+        double s = 0.0;
+        for (int t = 0; t < k; ++t) s += lrd[idx[i * k + t]];
+        scores[i] = s / ((double)k * lrd[i]);
+    }
+    free(xc);
+    free(idx);
+    free(dist);
+    free(lrd);
+    return 0;
 }

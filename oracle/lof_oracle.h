@@ -93,6 +93,24 @@ void oracle_ref_select_tile(const float* tile, const float* norms, int rows,
                             int64_t row_offset, int64_t n, int k, int32_t* nbr_idx,
                             float* nbr_d2, float* kdist2);
 
+/* oracle_knn_rows for an arbitrary list of m rows: rows[r]'s neighbours go
+ * to column r of the (k x m) outputs (slot t at [t * m + r]) and its
+ * k-distance to kdist2[r]. */
+void oracle_knn_list(const float* xc, int64_t n, int d, int k, const int64_t* rows, int64_t m,
+                     int32_t* nbr_idx, float* nbr_d2, float* kdist2, int nthreads);
+
+/* FP64 brute force from the definitions (Breunig et al. 2000), as the
+ * reference's cpu_lof (tests/cpp/test_culof.cu:39-80) computes them: the
+ * yardstick of the float32 engine's error, not a bit-exact restatement.
+ * oracle_knn_f64: the kk nearest of the m points rows[] (rows NULL: every
+ * point, m ignored) by (Euclidean distance, index), row-major (m x kk),
+ * ascending. oracle_lof_f64: the LOF scores. Both centre (and z-score) in
+ * double first. */
+void oracle_knn_f64(const float* x, int64_t n, int d, int normalize, int kk, const int64_t* rows,
+                    int64_t m, int64_t* idx, double* dist, int nthreads);
+int oracle_lof_f64(const float* x, int64_t n, int d, int k, int normalize, double* scores,
+                   int nthreads);
+
 #ifdef __cplusplus
 }
 #endif

@@ -19,7 +19,17 @@ Two kinds of golden data:
    reference's exact outputs for those scores, plus the messages of the
    ValueErrors its validation raises.
 
-Usage:  python tests/golden/make_golden.py [/path/to/reference]
+3. ``fullsize_clusters_n200000.npz``: scikit-learn's flagged set (packed
+   outlier bits at contamination 0.01), offset_ and the float32 scores of the
+   plain exact-LOF workload at full size (n = 200,000, d = 8, k = 20; the
+   seeded 5-cluster + 1% outlier generator, seed 1), which the GPU test of that
+   workload compares against (the reference's near-tie template,
+   test_parity.py:70-100, and its benchmark's agreement gate,
+   benchmarks/benchmark.py:102-116).
+
+Usage:  python tests/golden/make_golden.py --reference REF_ROOT [--only sklearn|layer|fullsize]
+(REF_ROOT is the reference's source tree, also taken from $CULOF_REFERENCE;
+only the ``layer`` fixtures read it.)
 """
 
 from __future__ import annotations
@@ -126,8 +136,39 @@ def make_reference_layer(path: str, ref_root: str) -> None:
     np.savez_compressed(path, **arrays)
 
 
+FULLSIZE = {"n": 200_000, "d": 8, "k": 20, "contamination": 0.01, "seed": 1}
+
+
+def make_fullsize(path: str) -> None:
+    from culof_gb300 import synthetic
+
+    f = FULLSIZE
+    X = synthetic.clusters_with_outliers(f["n"], f["d"], seed=f["seed"])
+    lof = LocalOutlierFactor(n_neighbors=f["k"], contamination=f["contamination"], n_jobs=-1)
+    labels = lof.fit_predict(X.astype(np.float64))
+    meta = dict(f, sha256=sha(X), offset=float(lof.offset_), n_outliers=int(np.sum(labels == -1)))
+    np.savez_compressed(
+        path,
+        outlier_bits=np.packbits(labels == -1),
+        scores=(-lof.negative_outlier_factor_).astype(np.float32),
+        meta_json=np.frombuffer(json.dumps(meta, sort_keys=True).encode(), dtype=np.uint8),
+    )
+
+
 if __name__ == "__main__":
-    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
-    make_sklearn_cases(os.path.join(HERE, "sklearn_cases.npz"))
-    make_reference_layer(os.path.join(HERE, "reference_python_layer.npz"), ref_root)
-    print("wrote", os.listdir(HERE))
+    import argparse
+
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--reference", default=os.environ.get("CULOF_REFERENCE"),
+                    help="the reference's source tree (needed for the 'layer' fixtures)")
+    ap.add_argument("--only", choices=["sklearn", "layer", "fullsize"])
+    a = ap.parse_args()
+    if a.only in (None, "sklearn"):
+        make_sklearn_cases(os.path.join(HERE, "sklearn_cases.npz"))
+    if a.only in (None, "layer"):
+        if not a.reference:
+            ap.error("--reference (or $CULOF_REFERENCE) is required for the reference-layer fixtures")
+        make_reference_layer(os.path.join(HERE, "reference_python_layer.npz"), a.reference)
+    if a.only in (None, "fullsize"):
+        make_fullsize(os.path.join(HERE, "fullsize_clusters_n200000.npz"))
+    print("wrote", sorted(os.listdir(HERE)))

@@ -89,9 +89,10 @@ def test_autograd_function_end_to_end():
 
 
 def test_backward_mixture_n50000_d32():
-    # n = 50,000, d = 32, k = 20: the sparse backward against FP64 autograd
-    # evaluated by torch on the GPU with the same neighbour slots
-    X = synthetic.clusters_with_outliers(50000, 32, seed=60)
+    # the gradient workload (8-cluster mixture, n = 50,000, d = 32, k = 20):
+    # the sparse backward against FP64 autograd evaluated by torch on the GPU
+    # with the same neighbour slots
+    X = synthetic.gradient_mixture(50000, 32, seed=60)
     w = np.random.default_rng(10).standard_normal(len(X))
     with _culof.Context() as ctx:
         idx, gx, _ = _gpu_grad(ctx, X, 20, False, w)
