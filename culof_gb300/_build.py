@@ -1,8 +1,10 @@
-"""Build libculof_gb300.so in-tree with nvcc for sm_103a (no cmake).
+"""Build libculof_gb300.so in-tree with nvcc for sm_103a (no cmake), and the
+compiled Python binding ``culof._culof`` over its C ABI with g++.
 
 Translation units compile in parallel into ``culof_gb300/_build/`` and link
-into ``culof_gb300/libculof_gb300.so``. A stamp of the sources and flags
-avoids rebuilding an up-to-date library.
+into ``culof_gb300/libculof_gb300.so``; ``culof/_culof.cpp`` compiles into
+``culof/_culof<EXT_SUFFIX>``, which finds the library through its run path.
+A stamp of the sources and flags avoids rebuilding up-to-date files.
 """
 
 from __future__ import annotations
@@ -12,6 +14,7 @@ import hashlib
 import os
 import shutil
 import subprocess
+import sysconfig
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
@@ -19,6 +22,8 @@ CSRC = os.path.join(HERE, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libculof_gb300.so")
+PYEXT_SRC = os.path.join(ROOT, "culof", "_culof.cpp")
+PYEXT = os.path.join(ROOT, "culof", "_culof" + (sysconfig.get_config_var("EXT_SUFFIX") or ".so"))
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = [
@@ -48,6 +53,7 @@ def _digest() -> str:
     files = sorted(
         [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
         + [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE)]
+        + [PYEXT_SRC]
     )
     for p in files:
         with open(p, "rb") as fh:
@@ -63,7 +69,7 @@ def build(force: bool = False, verbose: bool = False, jobs: int | None = None) -
     os.makedirs(BUILD, exist_ok=True)
     stamp = os.path.join(BUILD, "stamp")
     dig = _digest()
-    if not force and os.path.exists(LIB) and os.path.exists(stamp):
+    if not force and os.path.exists(LIB) and os.path.exists(PYEXT) and os.path.exists(stamp):
         with open(stamp) as fh:
             if fh.read().strip() == dig:
                 return LIB
@@ -87,9 +93,26 @@ def build(force: bool = False, verbose: bool = False, jobs: int | None = None) -
     if res.returncode != 0:
         raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")
     os.replace(tmp, LIB)
+    build_pyext()
     with open(stamp, "w") as fh:
         fh.write(dig)
     return LIB
+
+
+def build_pyext() -> str:
+    """culof/_culof.cpp -> culof/_culof<EXT_SUFFIX>, linked to the library
+    beside culof_gb300/ through a relative run path."""
+    tmp = PYEXT + f".tmp{os.getpid()}"
+    cmd = [
+        os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-shared", "-fPIC", "-fvisibility=hidden",
+        "-I", sysconfig.get_paths()["include"], "-I", INCLUDE, PYEXT_SRC, "-o", tmp,
+        "-L", HERE, "-lculof_gb300", "-Wl,-rpath,$ORIGIN/../culof_gb300",
+    ]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"building the Python binding failed:\n{res.stdout}\n{res.stderr}")
+    os.replace(tmp, PYEXT)
+    return PYEXT
 
 
 if __name__ == "__main__":

@@ -83,6 +83,9 @@ _SIGS = {
     "culof_context_pair_stats": ([_P, ctypes.POINTER(_D), ctypes.POINTER(_D)], _I),
     "culof_context_probe_bounded_wait": ([_P, ctypes.c_longlong], _I),
     "culof_compute_scores": ([_P, _P, _P, _I64, _I, _P], _I),
+    "culof_context_knn_shard_device": ([_P, _P, _I64, _I, _I, _I, _I, _I, _P, _P, _P, _P, ctypes.POINTER(_I64)], _I),
+    "culof_compute_lrd_rows": ([_P, _P, _P, _P, _I64, _I, _P, _I64, _P], _I),
+    "culof_compute_scores_rows": ([_P, _P, _P, _I64, _I, _P, _I64, _P], _I),
     "culof_context_contamination_offset_device": ([_P, _P, _I64, _D, _P], _I),
     "culof_contamination_offset_noalloc": ([_P, _P, _I64, _D, _P], _I),
     "culof_context_bf16_gram": ([_P, _P, _I64, _P, _I64, _I, _P], _I),
@@ -206,6 +209,16 @@ def compute_lrd(stream: int, nbr_idx: int, nbr_d2: int, kdist2: int, n_points: i
     _check(_lib.culof_compute_lrd(stream, nbr_idx, nbr_d2, kdist2, n_points, k, lrd))
 
 
+def compute_lrd_rows(stream: int, nbr_idx: int, nbr_d2: int, kdist2: int, n_points: int, k: int, rows: int,
+                     num_rows: int, lrd: int) -> None:
+    _check(_lib.culof_compute_lrd_rows(stream, nbr_idx, nbr_d2, kdist2, n_points, k, rows, num_rows, lrd))
+
+
+def compute_scores_rows(stream: int, nbr_idx: int, lrd: int, n_points: int, k: int, rows: int, num_rows: int,
+                        scores: int) -> None:
+    _check(_lib.culof_compute_scores_rows(stream, nbr_idx, lrd, n_points, k, rows, num_rows, scores))
+
+
 def compute_scores(stream: int, nbr_idx: int, lrd: int, n_points: int, k: int, scores: int) -> None:
     _check(_lib.culof_compute_scores(stream, nbr_idx, lrd, n_points, k, scores))
 
@@ -305,6 +318,15 @@ class Context:
                    kdist2: int) -> None:
         _check(_lib.culof_context_knn_device(self._h, points, n, d, int(k), int(bool(normalize)), nbr_idx, nbr_d2,
                                              kdist2))
+
+    def knn_shard_device(self, points: int, n: int, d: int, k: int, normalize: bool, shard: int, num_shards: int,
+                         nbr_idx: int, nbr_d2: int, kdist2: int, rows: int) -> int:
+        """One shard of a row-sharded k-NN; returns the number of rows it wrote."""
+        m = ctypes.c_int64(0)
+        _check(_lib.culof_context_knn_shard_device(self._h, points, n, d, int(k), int(bool(normalize)), int(shard),
+                                                   int(num_shards), nbr_idx, nbr_d2, kdist2, rows,
+                                                   ctypes.byref(m)))
+        return int(m.value)
 
     def lof_batched_device(self, offsets, ks, points: int, d: int, normalize: bool, scores: int) -> None:
         """LOF scores of many problems in one call (device points/scores,

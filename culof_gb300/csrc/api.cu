@@ -220,7 +220,7 @@ int culof_select_knn_tile(void* cuda_stream, float* d_tile, const float* d_norms
         if (rows < 0 || row_offset < 0 || row_offset + rows > n_points)
             throw Error(culof_gb300::kInvalidArgument, "rows out of range");
         if (k < 1 || k > n_points) throw Error(culof_gb300::kInvalidArgument, "k must satisfy 1 <= k <= n_points");
-        culof_gb300::radix_select_rows(d_tile, d_norms, rows, row_offset, n_points, k, culof_gb300::kSelectGram,
+        culof_gb300::select_tile_rows(d_tile, d_norms, rows, row_offset, n_points, k, culof_gb300::kSelectGram,
                                        d_nbr_idx, d_nbr_d2, d_kdist2, static_cast<cudaStream_t>(cuda_stream));
     });
 }
@@ -253,6 +253,43 @@ int culof_compute_scores(void* cuda_stream, const int32_t* d_nbr_idx, const floa
         if (n_points < 1 || k < 1) throw Error(culof_gb300::kInvalidArgument, "n_points and k must be >= 1");
         culof_gb300::compute_scores(d_nbr_idx, d_lrd, n_points, k, d_scores, nullptr, nullptr,
                                     static_cast<cudaStream_t>(cuda_stream));
+    });
+}
+
+int culof_context_knn_shard_device(culof_context* ctx, const float* d_points, int64_t n_points, int n_dims, int k,
+                                   int normalize, int shard, int num_shards, int32_t* d_nbr_idx, float* d_nbr_d2,
+                                   float* d_kdist2, int32_t* d_rows, int64_t* rows_out) {
+    return guarded([&] {
+        if (!d_nbr_idx || !d_nbr_d2 || !d_kdist2 || !d_rows)
+            throw Error(culof_gb300::kInvalidArgument, "device pointers must not be null");
+        const int64_t m = engine_of(ctx).knn_shard(d_points, n_points, n_dims, k, normalize != 0, shard, num_shards,
+                                                   d_nbr_idx, d_nbr_d2, d_kdist2, d_rows);
+        if (rows_out) *rows_out = m;
+    });
+}
+
+int culof_compute_lrd_rows(void* cuda_stream, const int32_t* d_nbr_idx, const float* d_nbr_d2,
+                           const float* d_kdist2, int64_t n_points, int k, const int32_t* d_rows, int64_t num_rows,
+                           float* d_lrd) {
+    return guarded([&] {
+        if (!d_nbr_idx || !d_nbr_d2 || !d_kdist2 || !d_lrd || !d_rows)
+            throw Error(culof_gb300::kInvalidArgument, "device pointers must not be null");
+        if (n_points < 1 || k < 1) throw Error(culof_gb300::kInvalidArgument, "n_points and k must be >= 1");
+        if (num_rows < 0 || num_rows > n_points) throw Error(culof_gb300::kInvalidArgument, "num_rows out of range");
+        culof_gb300::compute_lrd(d_nbr_idx, d_nbr_d2, d_kdist2, n_points, k, d_lrd, nullptr,
+                                 static_cast<cudaStream_t>(cuda_stream), d_rows, num_rows);
+    });
+}
+
+int culof_compute_scores_rows(void* cuda_stream, const int32_t* d_nbr_idx, const float* d_lrd, int64_t n_points,
+                              int k, const int32_t* d_rows, int64_t num_rows, float* d_scores) {
+    return guarded([&] {
+        if (!d_nbr_idx || !d_lrd || !d_scores || !d_rows)
+            throw Error(culof_gb300::kInvalidArgument, "device pointers must not be null");
+        if (n_points < 1 || k < 1) throw Error(culof_gb300::kInvalidArgument, "n_points and k must be >= 1");
+        if (num_rows < 0 || num_rows > n_points) throw Error(culof_gb300::kInvalidArgument, "num_rows out of range");
+        culof_gb300::compute_scores(d_nbr_idx, d_lrd, n_points, k, d_scores, nullptr, nullptr,
+                                    static_cast<cudaStream_t>(cuda_stream), d_rows, num_rows);
     });
 }
 

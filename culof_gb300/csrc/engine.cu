@@ -2,6 +2,7 @@
 // re-planned around a persistent context: one stream and grow-only
 // workspaces per context instead of seven cudaMallocs and a stream per call,
 // no cuBLAS, and a fused k-NN path whose n x n distances never reach HBM.
+#include <algorithm>
 #include <atomic>
 #include <cstdlib>
 #include <mutex>
@@ -163,18 +164,31 @@ int Engine::choose_path(int64_t n, int d, int k) const {
 }
 
 void Engine::knn_general(const float* xc, const float* norms, int64_t n, int d, int k,
-                         int32_t* nbr_idx, float* nbr_d2, float* kdist2) {
+                         int32_t* nbr_idx, float* nbr_d2, float* kdist2, int64_t row_begin, int64_t row_end) {
     const int tile = tile_rows_for(n);
     float* d_tile = tile_.as<float>(static_cast<size_t>(tile) * n);
-    for (int64_t row0 = 0; row0 < n; row0 += tile) {
-        const int rows = static_cast<int>((n - row0) < tile ? (n - row0) : tile);
+    for (int64_t row0 = row_begin; row0 < row_end; row0 += tile) {
+        const int rows = static_cast<int>((row_end - row0) < tile ? (row_end - row0) : tile);
         distance_tile(xc, n, d, row0, rows, d_tile, stream_);
-        radix_select_rows(d_tile, norms, rows, row0, n, k, kSelectDistances, nbr_idx, nbr_d2, kdist2, stream_);
+        select_tile_rows(d_tile, norms, rows, row0, n, k, kSelectDistances, nbr_idx, nbr_d2, kdist2, stream_);
     }
 }
 
 void Engine::knn(const float* d_x, int64_t n, int d, int k, bool normalize, int32_t* nbr_idx,
                  float* nbr_d2, float* kdist2) {
+    knn_core(d_x, n, d, k, normalize, 0, 1, nbr_idx, nbr_d2, kdist2, nullptr);
+}
+
+int64_t Engine::knn_shard(const float* d_x, int64_t n, int d, int k, bool normalize, int shard, int num_shards,
+                          int32_t* nbr_idx, float* nbr_d2, float* kdist2, int32_t* rows) {
+    if (num_shards < 1 || shard < 0 || shard >= num_shards)
+        throw Error(kInvalidArgument, "shard must satisfy 0 <= shard < num_shards");
+    if (rows == nullptr) throw Error(kInvalidArgument, "rows must not be null");
+    return knn_core(d_x, n, d, k, normalize, shard, num_shards, nbr_idx, nbr_d2, kdist2, rows);
+}
+
+int64_t Engine::knn_core(const float* d_x, int64_t n, int d, int k, bool normalize, int shard, int num_shards,
+                         int32_t* nbr_idx, float* nbr_d2, float* kdist2, int32_t* rows) {
     validate_lof_args(d_x, n, d, k);
     CG_CUDA(cudaSetDevice(device_));
     float* xc = xc_.as<float>(static_cast<size_t>(n) * d);
@@ -190,19 +204,30 @@ void Engine::knn(const float* d_x, int64_t n, int d, int k, bool normalize, int3
     center(d_x, n, d, normalize, xc, partial, mean, inv, stream_);
     squared_norms(xc, n, d, norms, maxn, stream_);
     const int path = choose_path(n, d, k);
+    int64_t count = n;
     if (path != kPathGeneral) {
         last_path_ = path;
         mark(1);
-        knn_fast(xc, norms, n, d, k, path == kPathTensor, nbr_idx, nbr_d2, kdist2);
+        knn_fast(xc, norms, n, d, k, path == kPathTensor, nbr_idx, nbr_d2, kdist2, shard, num_shards, rows);
+        if (num_shards > 1) {  // whole row tiles of 128 points
+            const int64_t nt = (n + 127) / 128;
+            const int64_t t0 = nt * shard / num_shards, t1 = nt * (shard + 1) / num_shards;
+            count = std::min<int64_t>(n, t1 * 128) - std::min<int64_t>(n, t0 * 128);
+        }
     } else {
         last_path_ = kPathGeneral;
         mark(1);
         mark(2);
         mark(3);
-        knn_general(xc, norms, n, d, k, nbr_idx, nbr_d2, kdist2);
+        // a shard of the general path: a block of original rows
+        const int64_t b = n * shard / num_shards, e = n * (shard + 1) / num_shards;
+        knn_general(xc, norms, n, d, k, nbr_idx, nbr_d2, kdist2, b, e);
+        if (rows && e > b) iota_rows(rows, b, e - b, stream_);
+        count = e - b;
         mark(4);
     }
     mark(5);
+    return count;
 }
 
 void Engine::lof_device(const float* d_x, int64_t n, int d, int k, bool normalize, float* d_scores,

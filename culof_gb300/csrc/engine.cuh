@@ -85,6 +85,14 @@ public:
     // Centre (+ z-score), norms and exact k-NN; outputs device, transposed.
     void knn(const float* d_x, int64_t n, int d, int k, bool normalize, int32_t* nbr_idx,
              float* nbr_d2, float* kdist2);
+    // One shard of a row-sharded k-NN: the neighbours of the shard's rows
+    // against all n points, written at the rows' own columns of the (k x n)
+    // outputs; rows (n capacity) receives the shard's original row indices.
+    // Returns their count. Shards of the fused paths are blocks of the
+    // spatial order's row tiles; the general path's are blocks of original
+    // rows. Every row's results equal the unsharded call's.
+    int64_t knn_shard(const float* d_x, int64_t n, int d, int k, bool normalize, int shard, int num_shards,
+                      int32_t* nbr_idx, float* nbr_d2, float* kdist2, int32_t* rows);
     // Positive LOF scores (and optionally nof = -scores) on the device.
     void lof_device(const float* d_x, int64_t n, int d, int k, bool normalize, float* d_scores,
                     float* d_nof);
@@ -122,9 +130,11 @@ private:
     void batch_autotune(const float* d_x, float* d_scores);
     int choose_path(int64_t n, int d, int k) const;
     void knn_general(const float* xc, const float* norms, int64_t n, int d, int k, int32_t* nbr_idx,
-                     float* nbr_d2, float* kdist2);
+                     float* nbr_d2, float* kdist2, int64_t row_begin, int64_t row_end);
     void knn_fast(const float* xc, const float* norms, int64_t n, int d, int k, bool tensor, int32_t* nbr_idx,
-                  float* nbr_d2, float* kdist2);
+                  float* nbr_d2, float* kdist2, int shard = 0, int num_shards = 1, int32_t* shard_rows = nullptr);
+    int64_t knn_core(const float* d_x, int64_t n, int d, int k, bool normalize, int shard, int num_shards,
+                     int32_t* nbr_idx, float* nbr_d2, float* kdist2, int32_t* rows);
     int tile_rows_for(int64_t n);
 
     int device_;

@@ -32,6 +32,7 @@
 // index), identical to the general path and the oracle; the filter only
 // decides which pairs get an exact evaluation, and its bound is proven
 // conservative (tau_from below).
+#include <algorithm>
 #include <cmath>
 #include <cstdlib>
 
@@ -412,12 +413,12 @@ __device__ __forceinline__ float box_gap2_rd(const float* __restrict__ a_lo, con
 
 // Keys for the launch order of the sweep: 0xFFFF - list length (ascending
 // sort = longest lists first), values the row tiles.
-__global__ void order_key_kernel(const int* __restrict__ pcount, int nt, unsigned* __restrict__ keys,
+__global__ void order_key_kernel(const int* __restrict__ pcount, int t0, int mt, unsigned* __restrict__ keys,
                                  unsigned* __restrict__ vals) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nt) return;
-    keys[t] = 0xFFFFu - static_cast<unsigned>(pcount[t]);
-    vals[t] = static_cast<unsigned>(t);
+    if (t >= mt) return;
+    keys[t] = 0xFFFFu - static_cast<unsigned>(pcount[t0 + t]);
+    vals[t] = static_cast<unsigned>(t0 + t);
 }
 
 // Per row tile T (one block): the column tiles that can hold a candidate for
@@ -425,14 +426,14 @@ __global__ void order_key_kernel(const int* __restrict__ pcount, int nt, unsigne
 // order, each with its rounded-down box gap (the sweep re-tests the gap
 // against its tighter current k-th distances without touching the boxes).
 template <int DP>
-__global__ void __launch_bounds__(256) prune_list_kernel(const float* __restrict__ boxes, int nt, int qs,
+__global__ void __launch_bounds__(256) prune_list_kernel(const float* __restrict__ boxes, int nt, int t0, int qs,
                                                          const unsigned long long* __restrict__ kth_seed,
                                                          uint2* __restrict__ plist, int* __restrict__ pcount) {
     __shared__ float tbox[2][DP];
     __shared__ float kmax_s;
     __shared__ int wtot[8];
     __shared__ int base_s;
-    const int T = blockIdx.x;
+    const int T = t0 + static_cast<int>(blockIdx.x);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (threadIdx.x < 2 * DP) tbox[threadIdx.x / DP][threadIdx.x % DP] = boxes[static_cast<int64_t>(T) * 2 * DP + threadIdx.x];
     if (warp == 0) {
@@ -484,12 +485,12 @@ __global__ void __launch_bounds__(256) prune_list_kernel(const float* __restrict
 }
 
 template <int DP>
-__global__ void __launch_bounds__(kThreads) seed_kernel(const float* __restrict__ tiles, int nt, int64_t n, int k,
-                                                        int qs, uint64_t* __restrict__ seed_keys,
+__global__ void __launch_bounds__(kThreads) seed_kernel(const float* __restrict__ tiles, int nt, int t0, int64_t n,
+                                                        int k, int qs, uint64_t* __restrict__ seed_keys,
                                                         unsigned long long* __restrict__ kth_shared) {
     __shared__ __align__(16) float tile[kSeedWindow][tile_floats(DP)];
     __shared__ uint64_t wl[kWarps][96];  // per warp: the row's sorted k best (k <= 64), then up to 32 new keys
-    const int T = blockIdx.x;
+    const int T = t0 + static_cast<int>(blockIdx.x);
     for (int q = 0; q < qs; ++q) {
         const float* src = tiles + static_cast<int64_t>(spiral_tile(T, q, nt)) * tile_floats(DP);
         for (int i = threadIdx.x; i < tile_floats(DP); i += kThreads) tile[q][i] = src[i];
@@ -696,7 +697,7 @@ __device__ bool drain_queue(SweepSmem<DP, M>& sh, int qc, const float* __restric
 // arrive by TMA and the last warp to finish a tile refills its stage.
 template <int DP, int M>
 __global__ void __launch_bounds__(kThreads, 2)
-sweep_kernel(const float* __restrict__ tiles, int nt, int qs, int nsplit, int k,
+sweep_kernel(const float* __restrict__ tiles, int nt, int t0, int mt, int qs, int nsplit, int k,
              const unsigned* __restrict__ max_norm_bits,
              unsigned long long* __restrict__ kth_shared, uint64_t* __restrict__ partial, int* __restrict__ status,
              unsigned long long* __restrict__ evaluated_blocks, const uint2* __restrict__ plist,
@@ -706,9 +707,10 @@ sweep_kernel(const float* __restrict__ tiles, int nt, int qs, int nsplit, int k,
     // row tiles with the longest candidate lists first (tail balance)
     // (split-major: a row tile's later splits start after its earlier ones
     // have shared their k-th keys, so they prune more)
-    const int ti = static_cast<int>(blockIdx.x) % nt;
-    const int T = order ? static_cast<int>(order[ti]) : ti;
-    const int split = static_cast<int>(blockIdx.x) / nt;
+    // (row tiles [t0, t0 + mt) of the nt: a shard of the rows)
+    const int ti = static_cast<int>(blockIdx.x) % mt;
+    const int T = order ? static_cast<int>(order[ti]) : t0 + ti;
+    const int split = static_cast<int>(blockIdx.x) / mt;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const float nmax = __uint_as_float(*max_norm_bits);
     const float* own = tiles + static_cast<int64_t>(T) * tile_floats(DP);
@@ -1014,15 +1016,15 @@ constexpr int kMergeWarps = 8;
 
 __global__ void __launch_bounds__(32 * kMergeWarps)
 merge_kernel(const uint64_t* __restrict__ seed_keys, const uint64_t* __restrict__ partial,
-             const unsigned* __restrict__ perm, int64_t n, int nt, int nsplit, int k, int32_t* __restrict__ nbr_idx,
-             float* __restrict__ nbr_d2, float* __restrict__ kdist2) {
+             const unsigned* __restrict__ perm, int64_t n, int nt, int64_t pos0, int64_t pos1, int nsplit, int k,
+             int32_t* __restrict__ nbr_idx, float* __restrict__ nbr_d2, float* __restrict__ kdist2) {
     extern __shared__ uint64_t msh[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int nl = nsplit + 1, total = nl * k;
     uint64_t* lists = msh + static_cast<int64_t>(warp) * (total + k);
     uint64_t* out = lists + total;
-    const int64_t pos = static_cast<int64_t>(blockIdx.x) * kMergeWarps + warp;
-    if (pos >= n) return;
+    const int64_t pos = pos0 + static_cast<int64_t>(blockIdx.x) * kMergeWarps + warp;
+    if (pos >= pos1) return;
     for (int e = lane; e < total; e += 32) {
         const int l = e / k, t = e % k;
         lists[e] = (l == 0) ? seed_keys[pos * k + t]
@@ -1091,26 +1093,27 @@ int choose_splits(int nt, int sms) {
 namespace {
 
 template <int DP, int M>
-void launch_sweep(const float* tiles, int nt, int qs, int nsplit, int k, const unsigned* maxn,
+void launch_sweep(const float* tiles, int nt, int t0, int mt, int qs, int nsplit, int k, const unsigned* maxn,
                   unsigned long long* kth_shared,
                   uint64_t* partial, int* status, unsigned long long* evaluated, const uint2* plist, const int* pcount,
                   const unsigned* order, const float* boxes, cudaStream_t s) {
     const size_t smem = sizeof(SweepSmem<DP, M>);
     set_max_dynamic_smem(reinterpret_cast<const void*>(sweep_kernel<DP, M>), static_cast<int>(smem));
-    sweep_kernel<DP, M><<<nt * nsplit, kThreads, smem, s>>>(tiles, nt, qs, nsplit, k, maxn, kth_shared, partial,
-                                                            status, evaluated, plist, pcount, order, boxes);
+    sweep_kernel<DP, M><<<mt * nsplit, kThreads, smem, s>>>(tiles, nt, t0, mt, qs, nsplit, k, maxn, kth_shared,
+                                                            partial, status, evaluated, plist, pcount, order, boxes);
     CG_LAUNCH_CHECK();
 }
 
 }  // namespace
 
 void launch_merge(const uint64_t* seed_keys, const uint64_t* partial, const unsigned* perm, int64_t n, int nt,
-                  int nsplit, int k, int32_t* idx, float* d2, float* kd, cudaStream_t s) {
+                  int64_t pos0, int64_t pos1, int nsplit, int k, int32_t* idx, float* d2, float* kd, cudaStream_t s) {
     const size_t smem = sizeof(uint64_t) * kMergeWarps * static_cast<size_t>((nsplit + 1) * k + k);
     if (smem > 48 * 1024)
         CG_CUDA(cudaFuncSetAttribute(merge_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
-    merge_kernel<<<static_cast<unsigned>(ceil_div(n, kMergeWarps)), 32 * kMergeWarps, smem, s>>>(
-        seed_keys, partial, perm, n, nt, nsplit, k, idx, d2, kd);
+    if (pos1 <= pos0) return;
+    merge_kernel<<<static_cast<unsigned>(ceil_div(pos1 - pos0, kMergeWarps)), 32 * kMergeWarps, smem, s>>>(
+        seed_keys, partial, perm, n, nt, pos0, pos1, nsplit, k, idx, d2, kd);
     CG_LAUNCH_CHECK();
 }
 
@@ -1150,12 +1153,16 @@ bool fast_path_supported(int64_t n, int d, int k) {
 
 // Host orchestration of the fast path.
 void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int k, bool tensor, int32_t* nbr_idx,
-                      float* nbr_d2, float* kdist2) {
+                      float* nbr_d2, float* kdist2, int shard, int num_shards, int32_t* shard_rows) {
     cudaStream_t s = stream_;
     const bool wide = !tensor && d > kMaxDP;
     const int dp = d <= 2 ? 2 : d <= 4 ? 4 : d <= 6 ? 6 : 8;
     const int nt = static_cast<int>(ceil_div(n, kCT));
     const int64_t padded = static_cast<int64_t>(nt) * kCT;
+    // the rows of this call: row tiles [t0, t0 + mt) of the spatial order
+    // (all of them unless the call is one shard of a row-sharded run)
+    const int t0 = static_cast<int>(static_cast<int64_t>(nt) * shard / num_shards);
+    const int mt = static_cast<int>(static_cast<int64_t>(nt) * (shard + 1) / num_shards) - t0;
     int sms = 152;
     CG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_));
     // The tensor sweep runs two CTAs per SM. Every split of a row tile starts
@@ -1167,17 +1174,18 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
     int nsplit = 1;
     if (nt > 1) {
         if (wide) {
-            nsplit = choose_splits(nt, sms);
+            nsplit = choose_splits(mt, sms);
+            if (nsplit > nt - 1) nsplit = nt - 1;
         } else if (!tensor) {
             // small-d sweep: about 9 waves of CTAs (2 per SM); more splits
             // only add merge work and restart more rows from the seed, fewer
             // leave the tail unbalanced (measured best: 7 splits at n = 50k,
             // 3 at 100k (3.33 ms against 3.73 ms with 7), 2 at 200k (8.85 ms
             // against 9.15 ms with 4))
-            nsplit = (18 * sms + nt / 2) / nt;
+            nsplit = mt > 0 ? (18 * sms + mt / 2) / mt : 1;
             nsplit = nsplit < 1 ? 1 : nsplit > 7 ? 7 : nsplit;
-        } else if (nt < 4 * sms) {
-            nsplit = (4 * sms + nt / 2) / nt;
+        } else if (mt < 4 * sms) {
+            nsplit = mt > 0 ? (4 * sms + mt / 2) / mt : 1;
             nsplit = nsplit < 1 ? 1 : nsplit > 3 ? 3 : nsplit;
             if (nsplit > nt - 1) nsplit = nt - 1;
         }
@@ -1224,6 +1232,11 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
         vout = t;
     }
     const unsigned* perm = vin;  // after 4 passes: back in the first half
+    const int64_t pos0 = static_cast<int64_t>(t0) * kCT;
+    const int64_t pos1 = std::min<int64_t>(n, static_cast<int64_t>(t0 + mt) * kCT);
+    if (shard_rows && pos1 > pos0)  // original indices of the shard's rows
+        CG_CUDA(cudaMemcpyAsync(shard_rows, perm + pos0, sizeof(unsigned) * (pos1 - pos0), cudaMemcpyDeviceToDevice,
+                                s));
 
     // 2. column tiles
     float* tiles = nullptr;
@@ -1268,13 +1281,13 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
     int* status = status_ptr();
     const unsigned* maxn = reinterpret_cast<const unsigned*>(max_norm_.get(sizeof(unsigned)));
     mark(2);
-    if (tensor) tc_seed(tcb, nt, d, k, seed_keys, kth_shared, s);
-    else if (wide) wide_seed(tiles, nt, d, k, seed_keys, kth_shared, s);
+    if (tensor) tc_seed(tcb, t0, mt, d, k, seed_keys, kth_shared, s);
+    else if (wide) wide_seed(tiles, nt, t0, mt, d, k, seed_keys, kth_shared, s);
     else switch (dp) {
-        case 2: seed_kernel<2><<<nt, kThreads, 0, s>>>(tiles, nt, n, k, qs, seed_keys, kth_shared); break;
-        case 4: seed_kernel<4><<<nt, kThreads, 0, s>>>(tiles, nt, n, k, qs, seed_keys, kth_shared); break;
-        case 6: seed_kernel<6><<<nt, kThreads, 0, s>>>(tiles, nt, n, k, qs, seed_keys, kth_shared); break;
-        default: seed_kernel<8><<<nt, kThreads, 0, s>>>(tiles, nt, n, k, qs, seed_keys, kth_shared); break;
+        case 2: seed_kernel<2><<<mt, kThreads, 0, s>>>(tiles, nt, t0, n, k, qs, seed_keys, kth_shared); break;
+        case 4: seed_kernel<4><<<mt, kThreads, 0, s>>>(tiles, nt, t0, n, k, qs, seed_keys, kth_shared); break;
+        case 6: seed_kernel<6><<<mt, kThreads, 0, s>>>(tiles, nt, t0, n, k, qs, seed_keys, kth_shared); break;
+        default: seed_kernel<8><<<mt, kThreads, 0, s>>>(tiles, nt, t0, n, k, qs, seed_keys, kth_shared); break;
     }
     if (!wide && !tensor) CG_LAUNCH_CHECK();
     mark(3);
@@ -1292,22 +1305,22 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
         plist = plist_.as<uint2>(static_cast<size_t>(nt) * nt);
         pcount = pcount_.as<int>(nt);
         switch (dp) {
-            case 2: prune_list_kernel<2><<<nt, 256, 0, s>>>(boxes, nt, qs, kth_shared, plist, pcount); break;
-            case 4: prune_list_kernel<4><<<nt, 256, 0, s>>>(boxes, nt, qs, kth_shared, plist, pcount); break;
-            case 6: prune_list_kernel<6><<<nt, 256, 0, s>>>(boxes, nt, qs, kth_shared, plist, pcount); break;
-            default: prune_list_kernel<8><<<nt, 256, 0, s>>>(boxes, nt, qs, kth_shared, plist, pcount); break;
+            case 2: prune_list_kernel<2><<<mt, 256, 0, s>>>(boxes, nt, t0, qs, kth_shared, plist, pcount); break;
+            case 4: prune_list_kernel<4><<<mt, 256, 0, s>>>(boxes, nt, t0, qs, kth_shared, plist, pcount); break;
+            case 6: prune_list_kernel<6><<<mt, 256, 0, s>>>(boxes, nt, t0, qs, kth_shared, plist, pcount); break;
+            default: prune_list_kernel<8><<<mt, 256, 0, s>>>(boxes, nt, t0, qs, kth_shared, plist, pcount); break;
         }
         CG_LAUNCH_CHECK();
     }
     // launch order: longest lists first (balances the tail of a many-wave
     // grid; small grids skip the sort)
-    if (plist && nt >= 4 * sms) {
-        unsigned* ok = reinterpret_cast<unsigned*>(order_.get(sizeof(unsigned) * (4 * static_cast<size_t>(nt) +
-                                                                                   sort_pairs_counts(nt))));
-        order_key_kernel<<<grid_for(nt, 256), 256, 0, s>>>(pcount, nt, ok, ok + nt);
+    if (plist && mt >= 4 * sms) {
+        unsigned* ok = reinterpret_cast<unsigned*>(order_.get(sizeof(unsigned) * (4 * static_cast<size_t>(mt) +
+                                                                                   sort_pairs_counts(mt))));
+        order_key_kernel<<<grid_for(mt, 256), 256, 0, s>>>(pcount, t0, mt, ok, ok + mt);
         CG_LAUNCH_CHECK();
         unsigned* sorted_vals = nullptr;
-        sort_pairs_stable(ok, ok + nt, ok + 2 * nt, ok + 3 * nt, nt, 16, ok + 4 * nt, s, &sorted_vals);
+        sort_pairs_stable(ok, ok + mt, ok + 2 * mt, ok + 3 * mt, mt, 16, ok + 4 * mt, s, &sorted_vals);
         order = sorted_vals;
     }
 
@@ -1315,19 +1328,19 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
     unsigned long long* evaluated = reinterpret_cast<unsigned long long*>(pair_stats_.get(2 * sizeof(unsigned long long)));
     CG_CUDA(cudaMemsetAsync(evaluated, 0, 2 * sizeof(unsigned long long), s));
     // every (warp, column tile) block past the seed window
-    stat_total_blocks_ = (!wide && !tensor && sweep) ? static_cast<unsigned long long>(nt) * (nt - qs) * kWarps : 0;
-    if (nt > 1 && tensor) {
-        uint64_t* lists = static_cast<uint64_t*>(tc_lists_.get(tc_list_bytes(nt, nsplit)));
-        tc_sweep(tcb, nt, nsplit, d, k, maxn, kth_shared, partial, lists, status, s);
-    } else if (nt > 1 && wide) {
-        wide_sweep(tiles, nt, nsplit, d, k, maxn, kth_shared, partial, s);
-    } else if (sweep) {
+    stat_total_blocks_ = (!wide && !tensor && sweep) ? static_cast<unsigned long long>(mt) * (nt - qs) * kWarps : 0;
+    if (nt > 1 && mt > 0 && tensor) {
+        uint64_t* lists = static_cast<uint64_t*>(tc_lists_.get(tc_list_bytes(mt, nsplit)));
+        tc_sweep(tcb, nt, t0, mt, nsplit, d, k, maxn, kth_shared, partial, lists, status, s);
+    } else if (nt > 1 && mt > 0 && wide) {
+        wide_sweep(tiles, nt, t0, mt, nsplit, d, k, maxn, kth_shared, partial, s);
+    } else if (sweep && mt > 0) {
         const bool big = k > 32;
-#define CG_SWEEP(DPV)                                                                                 \
-    (big ? launch_sweep<DPV, 96>(tiles, nt, qs, nsplit, k, maxn, kth_shared, partial, status, evaluated, plist, pcount, \
-                                 order, boxes, s)                                                                  \
-         : launch_sweep<DPV, 64>(tiles, nt, qs, nsplit, k, maxn, kth_shared, partial, status, evaluated, plist, pcount, \
-                                 order, boxes, s))
+#define CG_SWEEP(DPV)                                                                                              \
+    (big ? launch_sweep<DPV, 96>(tiles, nt, t0, mt, qs, nsplit, k, maxn, kth_shared, partial, status, evaluated, plist, \
+                                 pcount, order, boxes, s)                                                           \
+         : launch_sweep<DPV, 64>(tiles, nt, t0, mt, qs, nsplit, k, maxn, kth_shared, partial, status, evaluated, plist, \
+                                 pcount, order, boxes, s))
         switch (dp) {
             case 2: CG_SWEEP(2); break;
             case 4: CG_SWEEP(4); break;
@@ -1340,7 +1353,7 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
     mark(4);
 
     // 5. merge into the reference slot order
-    launch_merge(seed_keys, partial, perm, n, nt, ns, k, nbr_idx, nbr_d2, kdist2, s);
+    launch_merge(seed_keys, partial, perm, n, nt, pos0, pos1, ns, k, nbr_idx, nbr_d2, kdist2, s);
 }
 
 }  // namespace culof_gb300

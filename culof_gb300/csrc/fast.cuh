@@ -15,9 +15,11 @@ int wide_dims_padded(int d);
 size_t wide_tiles_floats(int d, int nt);
 void wide_build_tiles(const float* xc, const float* norms, int64_t n, int d, const unsigned* perm, int nt,
                       float* tiles, cudaStream_t s);
-void wide_seed(const float* tiles, int nt, int d, int k, uint64_t* seed_keys, unsigned long long* kth_shared,
-               cudaStream_t s);
-void wide_sweep(const float* tiles, int nt, int nsplit, int d, int k, const unsigned* maxn,
+// Row tiles [t0, t0 + mt) of the nt (every call covers a block of row tiles;
+// the whole problem is t0 = 0, mt = nt).
+void wide_seed(const float* tiles, int nt, int t0, int mt, int d, int k, uint64_t* seed_keys,
+               unsigned long long* kth_shared, cudaStream_t s);
+void wide_sweep(const float* tiles, int nt, int t0, int mt, int nsplit, int d, int k, const unsigned* maxn,
                 unsigned long long* kth_shared, uint64_t* partial, cudaStream_t s);
 
 // Stable LSD radix sort of (key, value) pairs on the low key_bits bits of the
@@ -32,8 +34,9 @@ void exclusive_scan_u32(unsigned* data, int64_t len, cudaStream_t s);
 
 // Shared by the FP32 and tensor-core sweeps (fast.cu).
 int choose_splits(int nt, int sms);
+// Merges the rows at sorted positions [pos0, pos1).
 void launch_merge(const uint64_t* seed_keys, const uint64_t* partial, const unsigned* perm, int64_t n, int nt,
-                  int nsplit, int k, int32_t* idx, float* d2, float* kd, cudaStream_t s);
+                  int64_t pos0, int64_t pos1, int nsplit, int k, int32_t* idx, float* d2, float* kd, cudaStream_t s);
 
 // The tensor-core variant (tc_sweep.cu). Sorted-order arrays of one call:
 // xh f16 operand rows [padded][Kp], xr FP32 coordinates [padded][dr], cn
@@ -51,11 +54,11 @@ size_t tc_buffer_bytes(int64_t padded, int d);
 // minmax: the per-dimension (min, max) keys of the spatial-order pass.
 TcBuffers tc_prepare(void* buf, const float* xc, const float* norms, int64_t n, int d, const unsigned* perm, int nt,
                      const unsigned* minmax, cudaStream_t s);
-void tc_seed(const TcBuffers& b, int nt, int d, int k, uint64_t* seed_keys, unsigned long long* kth_shared,
+void tc_seed(const TcBuffers& b, int t0, int mt, int d, int k, uint64_t* seed_keys, unsigned long long* kth_shared,
              cudaStream_t s);
 // Workspace of the per-row lists of one sweep launch batch.
 size_t tc_list_bytes(int nt, int nsplit);
-void tc_sweep(const TcBuffers& b, int nt, int nsplit, int d, int k, const unsigned* maxn,
+void tc_sweep(const TcBuffers& b, int nt, int t0, int mt, int nsplit, int d, int k, const unsigned* maxn,
               unsigned long long* kth_shared, uint64_t* partial, uint64_t* lists, int* status, cudaStream_t s);
 
 }  // namespace culof_gb300

@@ -18,11 +18,24 @@ namespace {
 
 constexpr int kBlock = 256;
 
+// One thread per point; `rows` (nullable) lists the m points of a row block
+// (a shard of a row-sharded run), otherwise every point.
+__device__ __forceinline__ int64_t block_row(const int32_t* rows, int64_t m, int64_t n, int* status) {
+    const int64_t r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (r >= m) return -1;
+    const int64_t i = rows ? static_cast<int64_t>(rows[r]) : r;
+    if (i < 0 || i >= n) {
+        if (status != nullptr) atomicExch(status, 2);
+        return -1;
+    }
+    return i;
+}
+
 __global__ void lrd_kernel(const int32_t* __restrict__ nbr_idx, const float* __restrict__ nbr_d2,
-                           const float* __restrict__ kdist2, int64_t n, int k,
-                           float* __restrict__ lrd, int* status) {
-    const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+                           const float* __restrict__ kdist2, int64_t n, int k, const int32_t* __restrict__ rows,
+                           int64_t m, float* __restrict__ lrd, int* status) {
+    const int64_t i = block_row(rows, m, n, status);
+    if (i < 0) return;
     if (status != nullptr && *status != 0) {
         lrd[i] = __int_as_float(0x7fc00000);
         return;
@@ -42,10 +55,10 @@ __global__ void lrd_kernel(const int32_t* __restrict__ nbr_idx, const float* __r
 }
 
 __global__ void score_kernel(const int32_t* __restrict__ nbr_idx, const float* __restrict__ lrd,
-                             int64_t n, int k, float* __restrict__ scores, float* __restrict__ nof,
-                             int* status) {
-    const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+                             int64_t n, int k, const int32_t* __restrict__ rows, int64_t m,
+                             float* __restrict__ scores, float* __restrict__ nof, int* status) {
+    const int64_t i = block_row(rows, m, n, status);
+    if (i < 0) return;
     const double self = static_cast<double>(lrd[i]);
     double sum = 0.0;
     for (int t = 0; t < k; ++t) {
@@ -196,16 +209,20 @@ int small_grid(int64_t n) {
 }  // namespace
 
 void compute_lrd(const int32_t* nbr_idx, const float* nbr_d2, const float* kdist2, int64_t n, int k,
-                 float* lrd, int* status, cudaStream_t s) {
-    lrd_kernel<<<static_cast<unsigned>(ceil_div(n, kBlock)), kBlock, 0, s>>>(nbr_idx, nbr_d2, kdist2, n, k, lrd,
-                                                                             status);
+                 float* lrd, int* status, cudaStream_t s, const int32_t* rows, int64_t m) {
+    if (!rows) m = n;
+    if (m <= 0) return;
+    lrd_kernel<<<static_cast<unsigned>(ceil_div(m, kBlock)), kBlock, 0, s>>>(nbr_idx, nbr_d2, kdist2, n, k, rows, m,
+                                                                             lrd, status);
     CG_LAUNCH_CHECK();
 }
 
 void compute_scores(const int32_t* nbr_idx, const float* lrd, int64_t n, int k, float* scores,
-                    float* nof, int* status, cudaStream_t s) {
-    score_kernel<<<static_cast<unsigned>(ceil_div(n, kBlock)), kBlock, 0, s>>>(nbr_idx, lrd, n, k, scores, nof,
-                                                                               status);
+                    float* nof, int* status, cudaStream_t s, const int32_t* rows, int64_t m) {
+    if (!rows) m = n;
+    if (m <= 0) return;
+    score_kernel<<<static_cast<unsigned>(ceil_div(m, kBlock)), kBlock, 0, s>>>(nbr_idx, lrd, n, k, rows, m, scores,
+                                                                               nof, status);
     CG_LAUNCH_CHECK();
 }
 

@@ -1,21 +1,21 @@
 // General exact k-NN path: an exact-distance tile (rows x n) written to HBM,
-// then an exact per-row radix select over it. It serves any k in [1, n-1]
-// and any d, and it is the engine's implementation of the reference's
-// internal tile contract (culof_internal.cuh:37-53: select_knn over a Gram
-// tile, knn.cu:119-241), which the tests drive with injected distances.
+// then an exact per-row select over it. It serves any k in [1, n-1] and any
+// d, and it is the engine's implementation of the reference's internal tile
+// contract (culof_internal.cuh:37-53: select_knn over a Gram tile), which the
+// tests drive with injected distances.
 //
-// The select keeps the reference's rules exactly:
+// Rules kept from the reference (the outputs must be the same bits):
 //   * key = IEEE bits of the non-negative squared distance, ordered as uint32;
-//   * three digit passes of 11, 11 and 10 bits pin down the k-th smallest key
-//     (knn.cu:136-184); that key's float is the k-distance;
-//   * the gather emits every key strictly below the k-th in ascending column
-//     index, then the keys equal to it in ascending column index until k slots
-//     are filled (knn.cu:190-231), via block prefix sums, no atomics on slots;
-//   * outputs are transposed: slot t of point i at [t * n + i].
-// In kSelectGram mode pass 0 converts a Gram value g to
-// max(0, (|x_self|^2 + |x_j|^2) - 2 g), with +inf for the diagonal and NaN,
-// and stores it back in place, as knn.cu:150-152 does. In kSelectDistances
-// mode the tile already holds exact distances and the diagonal is skipped.
+//     the k-distance is the float of the k-th smallest key (knn.cu:180-184);
+//   * slot order: every key strictly below the k-th in ascending column
+//     index, then the keys equal to it in ascending column index until k
+//     slots are filled (knn.cu:190-224);
+//   * outputs are transposed: slot t of point i at [t * n + i];
+//   * in kSelectGram mode a Gram value g becomes
+//     max(0, (|x_self|^2 + |x_j|^2) - 2 g), +inf for the diagonal and NaN,
+//     stored back in place (knn.cu:150-152); in kSelectDistances mode the
+//     tile already holds exact distances and the diagonal is skipped.
+// The select itself (row_select_kernel below) is this engine's own design.
 #include "block.cuh"
 #include "common.cuh"
 #include "prep.cuh"
@@ -76,139 +76,284 @@ distance_tile_kernel(const float* __restrict__ xc, int64_t n, int d, int64_t row
     }
 }
 
-constexpr int kSelBlock = 256;
-constexpr int kMaxBins = 2048;
+// ---------------------------------------------------------------- row select
+//
+// One CTA per row selects the row's k smallest keys (the IEEE bits of the
+// non-negative squared distance, ties by column index) and writes them in
+// slot order. The design:
+//   * each warp owns one contiguous segment of the row's columns and walks
+//     it 32 columns at a time, so every pass is coalesced and every loop is
+//     warp-uniform;
+//   * a 4096-bin histogram of the keys' bits 30..19 (bit 31 is always 0)
+//     built with warp-aggregated shared atomics (lanes with the same bin
+//     elect one adder) locates the bucket of the k-th key; a warp narrows the
+//     bins by ballots over lane prefix sums (4096 -> 128 -> 4 -> 1);
+//   * the keys of that bucket (typically a few hundred) are copied to shared
+//     memory with their columns and sorted (bitonic), which gives the k-th
+//     key; a bucket too large for the buffer is narrowed first by a second
+//     histogram (bits 18..7) and, if still too large, by a third (bits 6..0),
+//     which pins the k-th key's bits exactly;
+//   * every warp knows how many keys of its segment lie below the k-th key
+//     and how many equal it (from the extraction pass and the sorted bucket),
+//     so a warp-level exclusive scan gives each segment its first slot, and
+//     the emission pass ranks keys inside a 32-column step with ballots:
+//     keys below the k-th in ascending column order fill slots [0, below),
+//     keys equal to it fill [below, k) in ascending column order.
+// Rows of up to kRowCache keys stay in shared memory after the first pass.
 
-struct SelectShared {
-    int hist[kMaxBins];
-    int warp_sums[kSelBlock / 32];
-    unsigned int prefix;
-    int below;
-    int chunk;
-    int chunk_base;
-    int emitted_lt;
-    int emitted_eq;
+constexpr int kSelThreads = 256;
+constexpr int kSelWarps = kSelThreads / 32;
+constexpr int kBins = 4096;
+constexpr int kCandCap = 2048;
+constexpr int kRowCache = 4096;
+constexpr unsigned kFull = 0xffffffffu;
+
+struct RowSelect {
+    int hist[kBins];
+    unsigned long long cand[kCandCap];  // (key << 32) | column of the k-th key's bucket
+    int warp_lt[kSelWarps];             // keys of each warp's segment below the k-th key
+    int warp_eq[kSelWarps];             // keys equal to it
+    int ncand;
+    unsigned prefix;  // high bits of the k-th key found so far
+    int below;        // keys strictly below the current bucket
+    int need;         // rank of the k-th key inside the current bucket (1-based)
+    int bucket;       // keys inside the current bucket
 };
 
-// Find the bin of the need-th smallest key among the histogrammed ones and
-// fold it into the prefix: each thread owns bins/kSelBlock consecutive bins,
-// a block scan of their sums picks the owner, which walks its bins.
-__device__ void refine_prefix(SelectShared& sh, int bins, int shift, int need) {
-    const int per = bins / kSelBlock;
-    int local = 0;
-    for (int b = threadIdx.x * per; b < (threadIdx.x + 1) * per; ++b) local += sh.hist[b];
-    int total;
-    const int excl = block_exclusive_scan(local, sh.warp_sums, total);
-    if (excl < need && excl + local >= need) {
-        int acc = excl;
-        int bin = threadIdx.x * per;
-        for (int b = threadIdx.x * per; b < (threadIdx.x + 1) * per; ++b) {
-            if (acc + sh.hist[b] >= need) {
-                bin = b;
-                break;
-            }
-            acc += sh.hist[b];
-        }
-        sh.prefix |= static_cast<unsigned int>(bin) << shift;
-        sh.below += acc;
-    }
-    __syncthreads();
+// Levels of the bucket search: (lowest bit, width). Keys are < 2^31.
+__device__ __forceinline__ int level_shift(int lv) { return lv == 0 ? 19 : (lv == 1 ? 7 : 0); }
+__device__ __forceinline__ int level_width(int lv) { return lv == 2 ? 7 : 12; }
+
+// Adds 1 to hist[bin] for every lane with `take`; lanes that share a bin
+// elect one adder. All 32 lanes must call it.
+__device__ __forceinline__ void hist_add(int* hist, unsigned bin, bool take) {
+    const unsigned active = __ballot_sync(kFull, take);
+    if (!take) return;
+    const unsigned peers = __match_any_sync(active, bin);
+    if ((threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&hist[bin], __popc(peers));
 }
 
-__global__ void __launch_bounds__(kSelBlock)
-radix_select_kernel(float* __restrict__ tile, const float* __restrict__ norms, int rows,
-                    int64_t row_offset, int64_t n, int k, int mode, int32_t* __restrict__ nbr_idx,
-                    float* __restrict__ nbr_d2, float* __restrict__ kdist2) {
+// One warp: the bin holding the need-th key (1-based) of a histogram of
+// `bins` = 32 * 4^m entries. Each round splits the remaining range into 32
+// equal parts, one per lane, and keeps the part where the lanes' inclusive
+// prefix sums first reach `need` (a ballot). Returns the bin and sets the
+// keys below it and the keys inside it.
+__device__ int locate_bin(const int* hist, int bins, int need, int& below, int& inside) {
+    const int lane = threadIdx.x & 31;
+    int base = 0, span = bins, acc = 0;
+    while (true) {
+        const int part = span / 32 > 0 ? span / 32 : 1;
+        int s = 0;
+        if (lane * part < span)
+            for (int i = 0; i < part; ++i) s += hist[base + lane * part + i];
+        const int incl = warp_inclusive_scan(s);
+        const unsigned hit = __ballot_sync(kFull, acc + incl >= need);
+        const int L = hit ? __ffs(hit) - 1 : 31;  // counts are consistent: hit != 0
+        const int excl = __shfl_sync(kFull, incl - s, L);
+        const int own = __shfl_sync(kFull, s, L);
+        acc += excl;
+        base += L * part;
+        if (part == 1) {
+            below = acc;
+            inside = own;
+            return base;
+        }
+        span = part;
+    }
+}
+
+// Column j of the row as a key, from the shared-memory copy when the row
+// fits there.
+__device__ __forceinline__ unsigned row_key(const float* row, const unsigned* cache, bool cached, int64_t j) {
+    return cached ? cache[j] : __float_as_uint(row[j]);
+}
+
+__global__ void __launch_bounds__(kSelThreads)
+row_select_kernel(float* __restrict__ tile, const float* __restrict__ norms, int rows, int64_t row_offset,
+                  int64_t n, int k, int mode, int32_t* __restrict__ nbr_idx, float* __restrict__ nbr_d2,
+                  float* __restrict__ kdist2) {
+    __shared__ RowSelect sh;
+    extern __shared__ unsigned cache[];
     const int r = blockIdx.x;
     if (r >= rows) return;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const bool gram = (mode == kSelectGram);
+    const bool cached = n <= kRowCache;
     float* row = tile + static_cast<int64_t>(r) * n;
     const int64_t self = row_offset + r;
-    const bool gram = (mode == kSelectGram);
-    __shared__ SelectShared sh;
+    // warp segments: contiguous, a multiple of 32 columns each
+    const int64_t seg = ceil_div(ceil_div(n, kSelWarps), 32) * 32;
+    const int64_t s0 = static_cast<int64_t>(warp) * seg;
+    const int64_t s1 = s0 + seg < n ? s0 + seg : n;
+
+    for (int b = threadIdx.x; b < kBins; b += kSelThreads) sh.hist[b] = 0;
     if (threadIdx.x == 0) {
         sh.prefix = 0u;
         sh.below = 0;
-        sh.emitted_lt = 0;
-        sh.emitted_eq = 0;
+        sh.need = k;
     }
-    for (int b = threadIdx.x; b < kMaxBins; b += kSelBlock) sh.hist[b] = 0;
     __syncthreads();
 
-    // pass 0: top 11 bits (and the in-place Gram conversion)
+    // level 0 histogram (and the Gram conversion, written back in place)
     const float self_norm = gram ? norms[self] : 0.0f;
-    for (int64_t j = threadIdx.x; j < n; j += kSelBlock) {
-        unsigned int u;
-        if (gram) {
-            const float raw = __fsub_rn(__fadd_rn(self_norm, norms[j]), __fmul_rn(2.0f, row[j]));
-            const float d2 = (j == self || isnan(raw)) ? __int_as_float(0x7f800000) : fmaxf(0.0f, raw);
-            row[j] = d2;
-            u = __float_as_uint(d2);
-        } else {
-            if (j == self) continue;
-            u = __float_as_uint(row[j]);
+    for (int64_t j0 = s0; j0 < s1; j0 += 32) {
+        const int64_t j = j0 + lane;
+        const bool in = j < s1;
+        unsigned u = 0;
+        if (in) {
+            if (gram) {
+                const float raw = __fsub_rn(__fadd_rn(self_norm, norms[j]), __fmul_rn(2.0f, row[j]));
+                const float d2 = (j == self || isnan(raw)) ? __int_as_float(0x7f800000) : fmaxf(0.0f, raw);
+                row[j] = d2;
+                u = __float_as_uint(d2);
+            } else {
+                u = __float_as_uint(row[j]);
+            }
+            if (cached) cache[j] = u;
         }
-        atomicAdd(&sh.hist[u >> 21], 1);
+        // a point is never its own neighbour in distance mode; in Gram mode
+        // the diagonal is +inf and takes part, as the reference contract has it
+        hist_add(sh.hist, (u >> 19) & (kBins - 1), in && (gram || j != self));
     }
     __syncthreads();
-    refine_prefix(sh, 2048, 21, k);
 
-    // passes 1 and 2: the next 11 and the last 10 bits under the prefix
-    for (int p = 1; p < 3; ++p) {
-        const int shift = (p == 1) ? 10 : 0;
-        const int width = (p == 1) ? 11 : 10;
-        const int bins = 1 << width;
-        const unsigned int digit_mask = static_cast<unsigned int>(bins - 1);
-        const unsigned int hi_mask = 0xFFFFFFFFu << (shift + width);
-        const unsigned int prefix = sh.prefix;
-        const int need = k - sh.below;
-        for (int b = threadIdx.x; b < bins; b += kSelBlock) sh.hist[b] = 0;
-        __syncthreads();
-        for (int64_t j = threadIdx.x; j < n; j += kSelBlock) {
-            if (!gram && j == self) continue;
-            const unsigned int u = __float_as_uint(row[j]);
-            if ((u & hi_mask) == (prefix & hi_mask)) atomicAdd(&sh.hist[(u >> shift) & digit_mask], 1);
+    int level = 0;
+    while (true) {
+        if (warp == 0) {
+            int below = 0, inside = 0;
+            const int bin = locate_bin(sh.hist, 1 << level_width(level), sh.need, below, inside);
+            if (lane == 0) {
+                sh.prefix |= static_cast<unsigned>(bin) << level_shift(level);
+                sh.below += below;
+                sh.need -= below;
+                sh.bucket = inside;
+                sh.ncand = 0;
+            }
         }
         __syncthreads();
-        refine_prefix(sh, bins, shift, need);
+        if (sh.bucket <= kCandCap || level == 2) break;
+        // narrow the bucket with the next digit
+        ++level;
+        const int shift = level_shift(level);
+        const int hi = shift + level_width(level);
+        const unsigned want = sh.prefix >> hi;
+        for (int b = threadIdx.x; b < (1 << level_width(level)); b += kSelThreads) sh.hist[b] = 0;
+        __syncthreads();
+        for (int64_t j0 = s0; j0 < s1; j0 += 32) {
+            const int64_t j = j0 + lane;
+            const bool in = j < s1 && (gram || j != self);
+            const unsigned u = in ? row_key(row, cache, cached, j) : 0u;
+            hist_add(sh.hist, (u >> shift) & ((1u << level_width(level)) - 1u), in && (u >> hi) == want);
+        }
+        __syncthreads();
     }
-    const unsigned int kth = sh.prefix;
-    const int below = sh.below;
+
+    const int shift = level_shift(level);
+    const unsigned want = sh.prefix >> shift;
+    unsigned kth;
+    if (level == 2 && sh.bucket > kCandCap) {
+        // every key of the final bucket has the same bits: the k-th key
+        kth = sh.prefix;
+        int lt = 0, eq = 0;
+        for (int64_t j0 = s0; j0 < s1; j0 += 32) {
+            const int64_t j = j0 + lane;
+            const bool in = j < s1 && (gram || j != self);
+            const unsigned u = in ? row_key(row, cache, cached, j) : 0u;
+            lt += __popc(__ballot_sync(kFull, in && u < kth));
+            eq += __popc(__ballot_sync(kFull, in && u == kth));
+        }
+        if (lane == 0) {
+            sh.warp_lt[warp] = lt;
+            sh.warp_eq[warp] = eq;
+        }
+        __syncthreads();
+    } else {
+        // copy the bucket's keys with their columns; count the keys below it
+        int lt = 0;
+        for (int64_t j0 = s0; j0 < s1; j0 += 32) {
+            const int64_t j = j0 + lane;
+            const bool in = j < s1 && (gram || j != self);
+            const unsigned u = in ? row_key(row, cache, cached, j) : 0u;
+            const bool take = in && (u >> shift) == want;
+            lt += __popc(__ballot_sync(kFull, in && (u >> shift) < want));
+            const unsigned m = __ballot_sync(kFull, take);
+            int slot0 = 0;
+            if (lane == 0 && m) slot0 = atomicAdd(&sh.ncand, __popc(m));
+            slot0 = __shfl_sync(kFull, slot0, 0);
+            const int slot = slot0 + __popc(m & ((1u << lane) - 1u));
+            if (take && slot < kCandCap)
+                sh.cand[slot] = (static_cast<unsigned long long>(u) << 32) | static_cast<unsigned long long>(j);
+        }
+        if (lane == 0) {
+            sh.warp_lt[warp] = lt;
+            sh.warp_eq[warp] = 0;
+        }
+        __syncthreads();
+        // bitonic sort of the bucket, padded to a power of two with ~0
+        const int m = sh.ncand;
+        int len = 1;
+        while (len < m) len <<= 1;
+        for (int i = m + threadIdx.x; i < len; i += kSelThreads) sh.cand[i] = ~0ull;
+        __syncthreads();
+        for (int size = 2; size <= len; size <<= 1) {
+            for (int stride = size >> 1; stride > 0; stride >>= 1) {
+                for (int i = threadIdx.x; i < len / 2; i += kSelThreads) {
+                    const int lo = 2 * i - (i & (stride - 1));
+                    const int hi2 = lo + stride;
+                    const bool up = (lo & size) == 0;
+                    const unsigned long long a = sh.cand[lo], b = sh.cand[hi2];
+                    if ((a > b) == up) {
+                        sh.cand[lo] = b;
+                        sh.cand[hi2] = a;
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        kth = static_cast<unsigned>(sh.cand[sh.need - 1] >> 32);
+        // the bucket's keys below / equal to the k-th key, by owning warp
+        for (int i = threadIdx.x; i < m; i += kSelThreads) {
+            const unsigned u = static_cast<unsigned>(sh.cand[i] >> 32);
+            const int w = static_cast<int>(static_cast<int64_t>(sh.cand[i] & 0xffffffffull) / seg);
+            if (u < kth) atomicAdd(&sh.warp_lt[w], 1);
+            else if (u == kth) atomicAdd(&sh.warp_eq[w], 1);
+        }
+        __syncthreads();
+    }
+
+    // first slot of each segment: exclusive scans over the warps' counts
+    int lt_base = 0, eq_base = 0, below_all = 0;
+    {
+        const int my_lt = lane < kSelWarps ? sh.warp_lt[lane] : 0;
+        const int my_eq = lane < kSelWarps ? sh.warp_eq[lane] : 0;
+        const int lt_incl = warp_inclusive_scan(my_lt);
+        const int eq_incl = warp_inclusive_scan(my_eq);
+        lt_base = __shfl_sync(kFull, lt_incl - my_lt, warp);
+        eq_base = __shfl_sync(kFull, eq_incl - my_eq, warp);
+        below_all = __shfl_sync(kFull, lt_incl, kSelWarps - 1);
+    }
     if (threadIdx.x == 0) kdist2[self] = __uint_as_float(kth);
 
-    // ordered gather
-    for (int64_t base = 0; base < n; base += kSelBlock) {
-        const int64_t j = base + threadIdx.x;
-        const bool valid = j < n && (gram || j != self);
-        float v = 0.0f;
-        unsigned int u = 0xFFFFFFFFu;
-        if (valid) {
-            v = row[j];
-            u = __float_as_uint(v);
+    // ordered emission; a warp stops once its keys below the k-th are out
+    // and the tie slots are full
+    eq_base += below_all;
+    const int lt_end = lt_base + sh.warp_lt[warp];
+    for (int64_t j0 = s0; j0 < s1 && (lt_base < lt_end || eq_base < k); j0 += 32) {
+        const int64_t j = j0 + lane;
+        const bool in = j < s1 && (gram || j != self);
+        const unsigned u = in ? row_key(row, cache, cached, j) : 0u;
+        const bool is_lt = in && u < kth, is_eq = in && u == kth;
+        const unsigned mlt = __ballot_sync(kFull, is_lt), meq = __ballot_sync(kFull, is_eq);
+        const unsigned before = (1u << lane) - 1u;
+        int slot = -1;
+        if (is_lt) slot = lt_base + __popc(mlt & before);
+        if (is_eq) slot = eq_base + __popc(meq & before);
+        if (slot >= 0 && slot < k) {
+            nbr_idx[static_cast<int64_t>(slot) * n + self] = static_cast<int32_t>(j);
+            nbr_d2[static_cast<int64_t>(slot) * n + self] = __uint_as_float(u);
         }
-        const int lt = (valid && u < kth) ? 1 : 0;
-        const int eq = (valid && u == kth) ? 1 : 0;
-        int total;
-        const int off = block_exclusive_scan(lt | (eq << 16), sh.warp_sums, total);
-        if (lt) {
-            const int slot = sh.emitted_lt + (off & 0xFFFF);
-            if (slot < k) {
-                nbr_idx[static_cast<int64_t>(slot) * n + self] = static_cast<int32_t>(j);
-                nbr_d2[static_cast<int64_t>(slot) * n + self] = v;
-            }
-        }
-        if (eq) {
-            const int slot = below + sh.emitted_eq + (off >> 16);
-            if (slot < k) {
-                nbr_idx[static_cast<int64_t>(slot) * n + self] = static_cast<int32_t>(j);
-                nbr_d2[static_cast<int64_t>(slot) * n + self] = v;
-            }
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            sh.emitted_lt += total & 0xFFFF;
-            sh.emitted_eq += total >> 16;
-        }
-        __syncthreads();
+        lt_base += __popc(mlt);
+        eq_base += __popc(meq);
     }
 }
 
@@ -221,12 +366,28 @@ void distance_tile(const float* xc, int64_t n, int d, int64_t row0, int rows, fl
     CG_LAUNCH_CHECK();
 }
 
-void radix_select_rows(float* tile, const float* norms, int rows, int64_t row_offset, int64_t n,
-                       int k, int mode, int32_t* nbr_idx, float* nbr_d2, float* kdist2,
-                       cudaStream_t s) {
+void select_tile_rows(float* tile, const float* norms, int rows, int64_t row_offset, int64_t n, int k, int mode,
+                      int32_t* nbr_idx, float* nbr_d2, float* kdist2, cudaStream_t s) {
     if (rows <= 0) return;
-    radix_select_kernel<<<rows, kSelBlock, 0, s>>>(tile, norms, rows, row_offset, n, k, mode, nbr_idx,
-                                                    nbr_d2, kdist2);
+    set_max_dynamic_smem(reinterpret_cast<const void*>(row_select_kernel), kRowCache * sizeof(unsigned));
+    const int smem = n <= kRowCache ? static_cast<int>(n * sizeof(unsigned)) : 0;
+    row_select_kernel<<<rows, kSelThreads, smem, s>>>(tile, norms, rows, row_offset, n, k, mode, nbr_idx, nbr_d2,
+                                                      kdist2);
+    CG_LAUNCH_CHECK();
+}
+
+namespace {
+__global__ void iota_rows_kernel(int32_t* __restrict__ rows, int64_t first, int64_t m) {
+    for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < m;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+        rows[i] = static_cast<int32_t>(first + i);
+}
+}  // namespace
+
+void iota_rows(int32_t* rows, int64_t first, int64_t m, cudaStream_t s) {
+    int64_t g = ceil_div(m, 256);
+    if (g > 1024) g = 1024;
+    iota_rows_kernel<<<static_cast<unsigned>(g), 256, 0, s>>>(rows, first, m);
     CG_LAUNCH_CHECK();
 }
 

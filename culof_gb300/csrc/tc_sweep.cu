@@ -122,10 +122,10 @@ __global__ void tc_build_kernel(const float* __restrict__ xc, const float* __res
 // Per row of tile T: the exact k best keys over the tile's own columns and
 // the row's starting shared k-th key (as the FP32 seed kernels).
 __global__ void __launch_bounds__(256) tc_seed_kernel(const float* __restrict__ xr, const unsigned* __restrict__ ix,
-                                                      int d, int dr, int k, uint64_t* __restrict__ seed_keys,
+                                                      int t0, int d, int dr, int k, uint64_t* __restrict__ seed_keys,
                                                       unsigned long long* __restrict__ kth_shared) {
     extern __shared__ float spts[];  // [kCT][dr + 1]
-    const int T = blockIdx.x;
+    const int T = t0 + static_cast<int>(blockIdx.x);
     const int ld = dr + 1;  // odd stride: lanes reading different points hit different banks
     const int64_t base = static_cast<int64_t>(T) * kCT;
     for (int i = threadIdx.x; i < kCT * dr; i += blockDim.x) {
@@ -879,23 +879,23 @@ TcBuffers tc_prepare(void* buf, const float* xc, const float* norms, int64_t n, 
     return b;
 }
 
-void tc_seed(const TcBuffers& b, int nt, int d, int k, uint64_t* seed_keys, unsigned long long* kth_shared,
+void tc_seed(const TcBuffers& b, int t0, int mt, int d, int k, uint64_t* seed_keys, unsigned long long* kth_shared,
              cudaStream_t s) {
     const size_t smem = sizeof(float) * (static_cast<size_t>(kCT) * (b.dr + 1) + kCT);
     set_max_dynamic_smem(reinterpret_cast<const void*>(tc_seed_kernel), 100 * 1024);
-    tc_seed_kernel<<<nt, 256, smem, s>>>(b.xr, b.ix, d, b.dr, k, seed_keys, kth_shared);
+    tc_seed_kernel<<<mt, 256, smem, s>>>(b.xr, b.ix, t0, d, b.dr, k, seed_keys, kth_shared);
     CG_LAUNCH_CHECK();
 }
 
-void tc_sweep(const TcBuffers& b, int nt, int nsplit, int d, int k, const unsigned* maxn,
+void tc_sweep(const TcBuffers& b, int nt, int t0, int mt, int nsplit, int d, int k, const unsigned* maxn,
               unsigned long long* kth_shared, uint64_t* partial, uint64_t* lists, int* status, cudaStream_t s) {
     const size_t smem = sizeof(TcSmem) + 1024;
     set_max_dynamic_smem(reinterpret_cast<const void*>(tc_sweep_kernel), static_cast<int>(smem));
     const CUtensorMap map = tc::make_kmajor_map(b.xh, static_cast<int64_t>(nt) * kCT, b.Kp, true);
     // row tiles in batches, so that the list workspace stays bounded
     const int ntb_max = kTcMaxCtasPerLaunch / nsplit > 0 ? kTcMaxCtasPerLaunch / nsplit : 1;
-    for (int T0 = 0; T0 < nt; T0 += ntb_max) {
-        const int ntb = nt - T0 < ntb_max ? nt - T0 : ntb_max;
+    for (int T0 = t0; T0 < t0 + mt; T0 += ntb_max) {
+        const int ntb = t0 + mt - T0 < ntb_max ? t0 + mt - T0 : ntb_max;
         tc_sweep_kernel<<<ntb * nsplit, kTcThreads, smem, s>>>(map, b.xr, b.cn, b.ix,
                                                                reinterpret_cast<const TcScale*>(b.scale), nt, T0, ntb,
                                                                nsplit, d, b.dr, b.Kp, k, maxn, kth_shared, partial,

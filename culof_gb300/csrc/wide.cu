@@ -50,11 +50,11 @@ __global__ void build_wide_tiles_kernel(const float* __restrict__ xc, const floa
 
 // Per row of tile T: the exact k best keys over the tile's own columns and
 // the row's starting shared k-th key (as the small-d seed kernel).
-__global__ void __launch_bounds__(kThreads) wide_seed_kernel(const float* __restrict__ tiles, int nt, int d, int dpw,
+__global__ void __launch_bounds__(kThreads) wide_seed_kernel(const float* __restrict__ tiles, int t0, int d, int dpw,
                                                              int k, uint64_t* __restrict__ seed_keys,
                                                              unsigned long long* __restrict__ kth_shared) {
     extern __shared__ __align__(16) float stile[];  // [dpw][kCT] coords, then kCT index
-    const int T = blockIdx.x;
+    const int T = t0 + static_cast<int>(blockIdx.x);
     const float* src = tiles + static_cast<int64_t>(T) * wide_tile_floats(dpw);
     const int nfl = dpw * kCT;
     for (int i = threadIdx.x; i < nfl; i += kThreads) stile[i] = src[i];
@@ -150,15 +150,15 @@ __device__ bool wide_drain(WideHead<M>& H, const float* __restrict__ A, int qc, 
 
 template <int M>
 __global__ void __launch_bounds__(kThreads, 1)
-wide_sweep_kernel(const float* __restrict__ tiles, int nt, int nsplit, int d, int dpw, int k,
+wide_sweep_kernel(const float* __restrict__ tiles, int nt, int t0, int mt, int nsplit, int d, int dpw, int k,
                   const unsigned* __restrict__ max_norm_bits, unsigned long long* __restrict__ kth_shared,
                   uint64_t* __restrict__ partial) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     WideHead<M>& H = *reinterpret_cast<WideHead<M>*>(smem_raw);
     float* A = reinterpret_cast<float*>(smem_raw + ((sizeof(WideHead<M>) + 127) & ~size_t(127)));  // [dpw][kRT]
     float* B = A + dpw * kRT;                                                                        // [2][kChunk][kCT]
-    const int T = blockIdx.x % nt;
-    const int split = blockIdx.x / nt;
+    const int T = t0 + static_cast<int>(blockIdx.x) % mt;
+    const int split = static_cast<int>(blockIdx.x) / mt;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const float nmax = __uint_as_float(*max_norm_bits);
     const int64_t tfl = wide_tile_floats(dpw);
@@ -313,12 +313,13 @@ size_t wide_smem_bytes(int dpw) {
 }
 
 template <int M>
-void launch_wide_sweep_m(const float* tiles, int nt, int nsplit, int d, int dpw, int k, const unsigned* maxn,
-                         unsigned long long* kth_shared, uint64_t* partial, cudaStream_t s) {
+void launch_wide_sweep_m(const float* tiles, int nt, int t0, int mt, int nsplit, int d, int dpw, int k,
+                         const unsigned* maxn, unsigned long long* kth_shared, uint64_t* partial, cudaStream_t s) {
     const size_t smem = wide_smem_bytes<M>(dpw);
     CG_CUDA(cudaFuncSetAttribute(wide_sweep_kernel<M>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  static_cast<int>(smem)));
-    wide_sweep_kernel<M><<<nt * nsplit, kThreads, smem, s>>>(tiles, nt, nsplit, d, dpw, k, maxn, kth_shared, partial);
+    wide_sweep_kernel<M><<<mt * nsplit, kThreads, smem, s>>>(tiles, nt, t0, mt, nsplit, d, dpw, k, maxn, kth_shared,
+                                                             partial);
     CG_LAUNCH_CHECK();
 }
 
@@ -337,20 +338,21 @@ void wide_build_tiles(const float* xc, const float* norms, int64_t n, int d, con
     CG_LAUNCH_CHECK();
 }
 
-void wide_seed(const float* tiles, int nt, int d, int k, uint64_t* seed_keys, unsigned long long* kth_shared,
-               cudaStream_t s) {
+void wide_seed(const float* tiles, int nt, int t0, int mt, int d, int k, uint64_t* seed_keys,
+               unsigned long long* kth_shared, cudaStream_t s) {
+    (void)nt;
     const int dpw = wide_dims_padded(d);
     const size_t smem = sizeof(float) * (static_cast<size_t>(dpw) * kCT + kCT);
     CG_CUDA(cudaFuncSetAttribute(wide_seed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
-    wide_seed_kernel<<<nt, kThreads, smem, s>>>(tiles, nt, d, dpw, k, seed_keys, kth_shared);
+    wide_seed_kernel<<<mt, kThreads, smem, s>>>(tiles, t0, d, dpw, k, seed_keys, kth_shared);
     CG_LAUNCH_CHECK();
 }
 
-void wide_sweep(const float* tiles, int nt, int nsplit, int d, int k, const unsigned* maxn,
+void wide_sweep(const float* tiles, int nt, int t0, int mt, int nsplit, int d, int k, const unsigned* maxn,
                 unsigned long long* kth_shared, uint64_t* partial, cudaStream_t s) {
     const int dpw = wide_dims_padded(d);
-    if (k > 32) launch_wide_sweep_m<96>(tiles, nt, nsplit, d, dpw, k, maxn, kth_shared, partial, s);
-    else launch_wide_sweep_m<64>(tiles, nt, nsplit, d, dpw, k, maxn, kth_shared, partial, s);
+    if (k > 32) launch_wide_sweep_m<96>(tiles, nt, t0, mt, nsplit, d, dpw, k, maxn, kth_shared, partial, s);
+    else launch_wide_sweep_m<64>(tiles, nt, t0, mt, nsplit, d, dpw, k, maxn, kth_shared, partial, s);
 }
 
 }  // namespace culof_gb300

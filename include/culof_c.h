@@ -155,6 +155,42 @@ CULOF_API int culof_context_knn_device(culof_context* ctx, const float* d_points
                              int k, int normalize, int32_t* d_nbr_idx, float* d_nbr_d2,
                              float* d_kdist2);
 
+/* ---- row-sharded run (one rank per GPU; the multi-GPU plan) -----------
+ * The reference splits its k-NN stage into row tiles on one GPU
+ * (pipeline.cu:175-195); these entry points split it into shards across
+ * ranks. Each rank holds all n points and computes its shard's neighbours
+ * against all of them with no communication; the LOF then needs two
+ * exchanges of n floats: the k-distances before the LRD and the LRDs before
+ * the scores. Every entry is written by exactly one shard, so the exchange
+ * can be an all-reduce (sum) of zero-initialised n-float arrays, exact.
+ *
+ * culof_context_knn_shard_device: shard `shard` of num_shards (0 <= shard <
+ * num_shards) of culof_context_knn_device. The fused paths shard blocks of
+ * the engine's spatial order (row tiles of 128 points, the same order on
+ * every rank for the same points); the general path shards blocks of
+ * original rows. Outputs, device, written only at the shard's rows: slot t
+ * of point i at [t * n_points + i] of d_nbr_idx / d_nbr_d2 and d_kdist2[i];
+ * d_rows (n_points capacity) receives the shard's original row indices and
+ * *rows_out (host, nullable) their count. The shards of one problem list
+ * disjoint rows that cover all n, and each row's results are bit-identical
+ * to the unsharded call's. Asynchronous on the context stream. */
+CULOF_API int culof_context_knn_shard_device(culof_context* ctx, const float* d_points, int64_t n_points, int n_dims,
+                                             int k, int normalize, int shard, int num_shards, int32_t* d_nbr_idx,
+                                             float* d_nbr_d2, float* d_kdist2, int32_t* d_rows, int64_t* rows_out);
+
+/* include/culof_internal.cuh:56-58 compute_lrd (lof.cu:32-46) for a row
+ * block: the LRD of the num_rows points d_rows lists (d_lrd[i] for each
+ * listed i), given the (k x n) slots of those points and all n k-distances. */
+CULOF_API int culof_compute_lrd_rows(void* cuda_stream, const int32_t* d_nbr_idx, const float* d_nbr_d2,
+                                     const float* d_kdist2, int64_t n_points, int k, const int32_t* d_rows,
+                                     int64_t num_rows, float* d_lrd);
+
+/* include/culof_internal.cuh:60-62 compute_scores (lof.cu:49-62) for a row
+ * block: d_scores[i] for each listed i, given all n LRDs. */
+CULOF_API int culof_compute_scores_rows(void* cuda_stream, const int32_t* d_nbr_idx, const float* d_lrd,
+                                        int64_t n_points, int k, const int32_t* d_rows, int64_t num_rows,
+                                        float* d_scores);
+
 /* include/culof_internal.cuh:56-58 compute_lrd (lof.cu:32-46). Device pointers. */
 CULOF_API int culof_compute_lrd(void* cuda_stream, const int32_t* d_nbr_idx, const float* d_nbr_d2,
                       const float* d_kdist2, int64_t n_points, int k, float* d_lrd);

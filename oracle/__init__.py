@@ -78,6 +78,8 @@ def _load():
 
 
 def _ptr(a: np.ndarray) -> int:
+    """Address of a's data. The caller must hold a reference to `a` until the
+    C call returns (never pass a temporary conversion)."""
     return a.ctypes.data
 
 
@@ -127,18 +129,20 @@ def knn(Xc, k: int, rows=None, nthreads: int = 0):
 
 
 def lrd(nbr_idx, nbr_d2, kdist2) -> np.ndarray:
-    k, n = nbr_idx.shape
+    idx = np.ascontiguousarray(nbr_idx, np.int32)
+    d2, kd = _f32(nbr_d2), _f32(kdist2)
+    k, n = idx.shape
     out = np.empty(n, np.float32)
-    _load().oracle_lrd(
-        _ptr(np.ascontiguousarray(nbr_idx, np.int32)), _ptr(_f32(nbr_d2)), _ptr(_f32(kdist2)), n, k, _ptr(out)
-    )
+    _load().oracle_lrd(_ptr(idx), _ptr(d2), _ptr(kd), n, k, _ptr(out))
     return out
 
 
 def score(nbr_idx, lrd_) -> np.ndarray:
-    k, n = nbr_idx.shape
+    idx = np.ascontiguousarray(nbr_idx, np.int32)
+    lr = _f32(lrd_)
+    k, n = idx.shape
     out = np.empty(n, np.float32)
-    _load().oracle_score(_ptr(np.ascontiguousarray(nbr_idx, np.int32)), _ptr(_f32(lrd_)), n, k, _ptr(out))
+    _load().oracle_score(_ptr(idx), _ptr(lr), n, k, _ptr(out))
     return out
 
 
@@ -180,9 +184,8 @@ def ref_select_tile(tile, norms_, row_offset: int, k: int):
     idx = np.full((k, n), -1, np.int32)
     d2 = np.full((k, n), np.nan, np.float32)
     kd = np.full(n, np.nan, np.float32)
-    _load().oracle_ref_select_tile(
-        _ptr(tile), _ptr(_f32(norms_)), rows, row_offset, n, k, _ptr(idx), _ptr(d2), _ptr(kd)
-    )
+    nrm = _f32(norms_)
+    _load().oracle_ref_select_tile(_ptr(tile), _ptr(nrm), rows, row_offset, n, k, _ptr(idx), _ptr(d2), _ptr(kd))
     return idx, d2, kd
 
 

@@ -49,30 +49,62 @@ def test_choose_tile_rows_respects_budget():
     assert _culof.choose_tile_rows(1000, 1 << 40) == 1000
 
 
-def test_version_and_surface(ref_layer_golden):
+@pytest.mark.parametrize("pkg", ["culof_gb300", "culof"])
+def test_version_and_surface(pkg, ref_layer_golden):
+    import importlib
+
+    mod = importlib.import_module(pkg)
     meta = ref_layer_golden.meta
-    assert culof_gb300.__version__ == meta["version"] == _culof.version()
-    assert sorted(culof_gb300.__all__) == sorted(meta["all"])
-    assert repr(LOF(n_neighbors=7)) == meta["repr"]
+    assert mod.__version__ == meta["version"] == _culof.version()
+    assert sorted(mod.__all__) == sorted(meta["all"])
+    assert repr(mod.LOF(n_neighbors=7)) == meta["repr"]
+    for name in mod.__all__:
+        assert hasattr(mod, name), name
+
+
+def test_compiled_binding_module():
+    # culof._culof: the compiled counterpart of the reference's pybind11
+    # module (binding.cpp:47-56), over the C ABI
+    import sysconfig
+
+    import culof
+    from culof import _culof as native
+
+    assert native.__file__.endswith(sysconfig.get_config_var("EXT_SUFFIX"))
+    for name in ("lof", "fit_predict", "cuda_available", "device_info", "CudaError"):
+        assert hasattr(native, name), name
+    assert issubclass(native.CudaError, RuntimeError) and culof.CudaError is native.CudaError
+    assert isinstance(native.cuda_available(), bool)
+    with pytest.raises(ValueError, match="2-D array"):
+        native.lof(np.zeros(10, np.float32), 3, False)
+    with pytest.raises(ValueError, match="2-D array"):
+        native.lof(np.zeros((2, 3, 4), np.float32), 3, False)
+    with pytest.raises(ValueError, match="contamination"):
+        native.fit_predict(np.zeros((10, 2), np.float32), 3, False, -0.5)
+    with pytest.raises(TypeError):
+        native.lof(np.zeros((10, 2), np.float32), "three", False)
 
 
 @pytest.mark.parametrize(
     "label,call",
     [
-        ("k0", lambda: LOF(n_neighbors=0)),
-        ("contam_bad", lambda: LOF(contamination=0.9)),
-        ("k_too_big", lambda: LOF(n_neighbors=100).fit(np.zeros((100, 2), np.float32))),
-        ("not_2d", lambda: lof(np.zeros(10, np.float32), 3)),
-        ("nan", lambda: lof(np.array([[0.0, np.nan], [1.0, 1.0], [2.0, 2.0]], np.float32), 1)),
-        ("overflow", lambda: lof((np.ones((64, 4)) * 1e20).astype(np.float32), 5)),
-        ("no_features", lambda: lof(np.zeros((5, 0), np.float32), 1)),
-        ("unfitted", lambda: LOF().predict()),
+        ("k0", lambda m: m.LOF(n_neighbors=0)),
+        ("contam_bad", lambda m: m.LOF(contamination=0.9)),
+        ("k_too_big", lambda m: m.LOF(n_neighbors=100).fit(np.zeros((100, 2), np.float32))),
+        ("not_2d", lambda m: m.lof(np.zeros(10, np.float32), 3)),
+        ("nan", lambda m: m.lof(np.array([[0.0, np.nan], [1.0, 1.0], [2.0, 2.0]], np.float32), 1)),
+        ("overflow", lambda m: m.lof((np.ones((64, 4)) * 1e20).astype(np.float32), 5)),
+        ("no_features", lambda m: m.lof(np.zeros((5, 0), np.float32), 1)),
+        ("unfitted", lambda m: m.LOF().predict()),
     ],
 )
-def test_validation_messages_match_reference(label, call, ref_layer_golden):
+@pytest.mark.parametrize("pkg", ["culof_gb300", "culof"])
+def test_validation_messages_match_reference(pkg, label, call, ref_layer_golden):
+    import importlib
+
     kind, msg = ref_layer_golden.meta["errors"][label]
     with pytest.raises(ValueError) as ei:
-        call()
+        call(importlib.import_module(pkg))
     assert type(ei.value).__name__ == kind
     assert str(ei.value) == msg
 
