@@ -130,8 +130,10 @@ int Engine::tile_rows_for(int64_t n) {
 }
 
 // AUTO: the general tile + select path for n <= 4096 (a few kernels against
-// the fused paths' ~45: n = 1000, d = 8: 0.12 ms against 0.37 ms) and beyond
-// the fused paths' limits (d > 128 or k > 64); otherwise the FP32 fused
+// the fused paths' ~45; fit_predict on the device, d = 8, k = 20: n = 1000,
+// 0.18 ms against 0.38 ms; n = 4000, 0.39 against 0.58 ms; n = 8000, 1.02
+// against 0.62 ms) and beyond the fused paths' limits (d > 128 or k > 64);
+// otherwise the FP32 fused
 // sweep for d <= 8 and the tensor-core sweep for 8 < d <= 128 (the FP32 wide
 // sweep for d <= 16 below one wave of row tiles). All give the same bits.
 // CULOF_GB300_PATH=general|fast|tensor overrides AUTO for a process.
