@@ -94,6 +94,8 @@ def parse_args():
     p.add_argument("--batched", type=int, default=0, metavar="N",
                    help="the batched problem mix (d = 16, k 10-40, n log-uniform in [128, 16384]) with N problems, "
                         "batched call against single calls")
+    p.add_argument("--backward", action="store_true",
+                   help="the gradient workload alone (mixture, --n/--d/--k): forward + sparse backward timing")
     p.add_argument("--scaling", action="store_true",
                    help="the reference benchmark's n and d sweeps through culof_gb300.lof, gated bit-exact on the oracle")
     p.add_argument("--workload", choices=["clusters", "factor", "mixture"], default="clusters",
@@ -740,12 +742,54 @@ def run_batched(args):
     return 0
 
 
+def run_backward(args):
+    """The gradient workload alone (8-cluster mixture, --n points, --d dims,
+    --k neighbours): forward and sparse backward of sum_i w_i LOF_i through
+    the autograd function, timed with CUDA events, the gradient compared with
+    FP64 autograd of the same fixed-neighbour LOF."""
+    import torch
+
+    from culof_gb300 import _culof
+    from culof_gb300.autograd import lof_scores
+    from oracle import backward as ob
+
+    torch.cuda.set_device(0)
+    stream = torch.cuda.current_stream()
+    X = load_synthetic().gradient_mixture(args.n, args.d, seed=args.seed)
+    w = torch.from_numpy(np.random.default_rng(3).standard_normal(len(X))).cuda()
+    Xt = torch.from_numpy(X).cuda()
+
+    def fwd_bwd():
+        Xg = Xt.clone().requires_grad_(True)
+        (lof_scores(Xg, args.k).double() * w).sum().backward()
+        return Xg.grad
+
+    ms_fb = _time_calls(fwd_bwd, stream, warm=args.warmup, reps=args.steps)
+    ms_f = _time_calls(lambda: lof_scores(Xt, args.k), stream, warm=args.warmup, reps=args.steps)
+    g = fwd_bwd().double()
+    with _culof.Context() as ctx:
+        idx = torch.empty((args.k, len(X)), dtype=torch.int32, device="cuda")
+        d2 = torch.empty((args.k, len(X)), device="cuda")
+        kd = torch.empty(len(X), device="cuda")
+        ctx.knn_device(Xt.data_ptr(), len(X), args.d, args.k, False, idx.data_ptr(), d2.data_ptr(), kd.data_ptr())
+        ctx.synchronize()
+    X64 = Xt.double().requires_grad_(True)
+    (ob.lof_fixed(X64, idx.long(), False) * w).sum().backward()
+    rel = float((g - X64.grad).abs().max() / X64.grad.abs().max())
+    print(json.dumps({"workload": f"gradient mixture n={len(X)} d={args.d} k={args.k}", "forward_s": ms_f * 1e-3,
+                      "backward_s": (ms_fb - ms_f) * 1e-3, "forward_backward_s": ms_fb * 1e-3,
+                      "grad_max_rel_err_vs_fp64_autograd": rel, "device": _culof.device_info()}), flush=True)
+    return 0
+
+
 def main():
     args = parse_args()
     if args.suite:
         return run_suite(args)
     if args.batched:
         return run_batched(args)
+    if args.backward:
+        return run_backward(args)
     if args.scaling:
         return run_scaling(args)
     if args.impl == "reference":
