@@ -163,7 +163,7 @@ private:
     cudaStream_t bgraph_stream_ = nullptr;
     unsigned long long bgraph_kernels_ = 0;
     // fast path workspaces
-    DevBuf morton_, perm_, sort_tmp_, sort_hist_, cols_, rows_, tc_lists_;
+    DevBuf morton_, perm_, sort_tmp_, sort_hist_, cols_, rows_, tc_lists_, tiles_;
     // the FP32 sweep's evaluated (warp x column tile) blocks; the total it
     // would evaluate without pruning
     DevBuf pair_stats_, boxes_, plist_, pcount_, order_;

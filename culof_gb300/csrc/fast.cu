@@ -1156,6 +1156,10 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
                       float* nbr_d2, float* kdist2, int shard, int num_shards, int32_t* shard_rows) {
     cudaStream_t s = stream_;
     const bool wide = !tensor && d > kMaxDP;
+    // the tensor sweep for d <= 8 starts from the small-d seed window and
+    // visits only the column tiles of the small-d prune lists
+    const bool small_tc = tensor && d <= kMaxDP;
+    const bool small = !wide && (!tensor || small_tc);  // FP32 small-d tiles, boxes and seed
     const int dp = d <= 2 ? 2 : d <= 4 ? 4 : d <= 6 ? 6 : 8;
     const int nt = static_cast<int>(ceil_div(n, kCT));
     const int64_t padded = static_cast<int64_t>(nt) * kCT;
@@ -1196,7 +1200,7 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
     }
     // the small-d seed covers the first qs spiral positions of every row
     // tile, the sweep the rest (the wide and tensor seeds cover tile T alone)
-    const int qs = (wide || tensor) ? 1 : (nt < kSeedWindow ? nt : kSeedWindow);
+    const int qs = small ? (nt < kSeedWindow ? nt : kSeedWindow) : 1;
     const bool sweep = nt > qs;
     if (sweep && nsplit > nt - qs) nsplit = nt - qs;  // no split without a column tile
 
@@ -1242,24 +1246,24 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
     float* tiles = nullptr;
     TcBuffers tcb{};
     float* boxes = nullptr;
-    if (tensor) {
-        tcb = tc_prepare(cols_.get(tc_buffer_bytes(padded, d)), xc, norms, n, d, perm, nt, mm, s);
-    } else if (wide) {
+    if (tensor) tcb = tc_prepare(cols_.get(tc_buffer_bytes(padded, d)), xc, norms, n, d, perm, nt, mm, s);
+    DevBuf& small_tiles = small_tc ? tiles_ : cols_;
+    if (wide) {
         tiles = cols_.as<float>(wide_tiles_floats(d, nt));
         wide_build_tiles(xc, norms, n, d, perm, nt, tiles, s);
-    } else switch (dp) {
-        case 2: tiles = cols_.as<float>(static_cast<size_t>(tile_floats(2)) * nt); break;
-        case 4: tiles = cols_.as<float>(static_cast<size_t>(tile_floats(4)) * nt); break;
-        case 6: tiles = cols_.as<float>(static_cast<size_t>(tile_floats(6)) * nt); break;
-        default: tiles = cols_.as<float>(static_cast<size_t>(tile_floats(8)) * nt); break;
+    } else if (small) switch (dp) {
+        case 2: tiles = small_tiles.as<float>(static_cast<size_t>(tile_floats(2)) * nt); break;
+        case 4: tiles = small_tiles.as<float>(static_cast<size_t>(tile_floats(4)) * nt); break;
+        case 6: tiles = small_tiles.as<float>(static_cast<size_t>(tile_floats(6)) * nt); break;
+        default: tiles = small_tiles.as<float>(static_cast<size_t>(tile_floats(8)) * nt); break;
     }
-    if (!wide && !tensor) switch (dp) {
+    if (small) switch (dp) {
         case 2: build_tiles_kernel<2><<<grid_for(padded, 256), 256, 0, s>>>(xc, norms, n, d, perm, padded, tiles); break;
         case 4: build_tiles_kernel<4><<<grid_for(padded, 256), 256, 0, s>>>(xc, norms, n, d, perm, padded, tiles); break;
         case 6: build_tiles_kernel<6><<<grid_for(padded, 256), 256, 0, s>>>(xc, norms, n, d, perm, padded, tiles); break;
         default: build_tiles_kernel<8><<<grid_for(padded, 256), 256, 0, s>>>(xc, norms, n, d, perm, padded, tiles); break;
     }
-    if (!wide && !tensor) {
+    if (small) {
         CG_LAUNCH_CHECK();
         boxes = boxes_.as<float>(static_cast<size_t>(nt) * 2 * dp);
         const unsigned bg = static_cast<unsigned>(ceil_div(nt, 8));
@@ -1281,7 +1285,7 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
     int* status = status_ptr();
     const unsigned* maxn = reinterpret_cast<const unsigned*>(max_norm_.get(sizeof(unsigned)));
     mark(2);
-    if (tensor) tc_seed(tcb, t0, mt, d, k, seed_keys, kth_shared, s);
+    if (tensor && !small_tc) tc_seed(tcb, t0, mt, d, k, seed_keys, kth_shared, s);
     else if (wide) wide_seed(tiles, nt, t0, mt, d, k, seed_keys, kth_shared, s);
     else switch (dp) {
         case 2: seed_kernel<2><<<mt, kThreads, 0, s>>>(tiles, nt, t0, n, k, qs, seed_keys, kth_shared); break;
@@ -1289,7 +1293,7 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
         case 6: seed_kernel<6><<<mt, kThreads, 0, s>>>(tiles, nt, t0, n, k, qs, seed_keys, kth_shared); break;
         default: seed_kernel<8><<<mt, kThreads, 0, s>>>(tiles, nt, t0, n, k, qs, seed_keys, kth_shared); break;
     }
-    if (!wide && !tensor) CG_LAUNCH_CHECK();
+    if (small) CG_LAUNCH_CHECK();
     mark(3);
 
     // 3b. per row tile: the column tiles the seed's k-th distances leave
@@ -1301,7 +1305,7 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
     // limit do (the same results; it puts that path within reach of tests)
     const char* lists_env = std::getenv("CULOF_PRUNE_LISTS");
     const bool lists_on = !(lists_env && lists_env[0] == '0');
-    if (!wide && !tensor && sweep && nt <= kMaxListTiles && lists_on) {
+    if (small && sweep && nt <= kMaxListTiles && lists_on) {
         plist = plist_.as<uint2>(static_cast<size_t>(nt) * nt);
         pcount = pcount_.as<int>(nt);
         switch (dp) {
@@ -1314,7 +1318,7 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
     }
     // launch order: longest lists first (balances the tail of a many-wave
     // grid; small grids skip the sort)
-    if (plist && mt >= 4 * sms) {
+    if (plist && !tensor && mt >= 4 * sms) {
         unsigned* ok = reinterpret_cast<unsigned*>(order_.get(sizeof(unsigned) * (4 * static_cast<size_t>(mt) +
                                                                                    sort_pairs_counts(mt))));
         order_key_kernel<<<grid_for(mt, 256), 256, 0, s>>>(pcount, t0, mt, ok, ok + mt);
@@ -1328,10 +1332,10 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
     unsigned long long* evaluated = reinterpret_cast<unsigned long long*>(pair_stats_.get(2 * sizeof(unsigned long long)));
     CG_CUDA(cudaMemsetAsync(evaluated, 0, 2 * sizeof(unsigned long long), s));
     // every (warp, column tile) block past the seed window
-    stat_total_blocks_ = (!wide && !tensor && sweep) ? static_cast<unsigned long long>(mt) * (nt - qs) * kWarps : 0;
-    if (nt > 1 && mt > 0 && tensor) {
+    stat_total_blocks_ = (small && !tensor && sweep) ? static_cast<unsigned long long>(mt) * (nt - qs) * kWarps : 0;
+    if (sweep && mt > 0 && tensor) {
         uint64_t* lists = static_cast<uint64_t*>(tc_lists_.get(tc_list_bytes(mt, nsplit)));
-        tc_sweep(tcb, nt, t0, mt, nsplit, d, k, maxn, kth_shared, partial, lists, status, s);
+        tc_sweep(tcb, nt, t0, mt, nsplit, d, k, maxn, kth_shared, partial, lists, status, s, qs, plist, pcount);
     } else if (nt > 1 && mt > 0 && wide) {
         wide_sweep(tiles, nt, t0, mt, nsplit, d, k, maxn, kth_shared, partial, s);
     } else if (sweep && mt > 0) {

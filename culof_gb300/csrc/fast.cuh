@@ -41,14 +41,23 @@ void launch_merge(const uint64_t* seed_keys, const uint64_t* partial, const unsi
 // The tensor-core variant (tc_sweep.cu). Sorted-order arrays of one call:
 // xh f16 operand rows [padded][Kp], xr FP32 coordinates [padded][dr], cn
 // norms, ix original indices, scale a device record of the f16 scaling.
+// split: each coordinate x (scaled) is carried as two f16 values, hi =
+// f16(x) and lo = f16(x - hi); the row operand holds [hi, lo, hi] and the
+// column operand [hi, hi, lo] (d values each), so their product sums
+// hi.hi + lo.hi + hi.lo, the Gram value to about 2^-22 relative instead of
+// 2^-11 (used when 3d <= 128); xb is then the column-arrangement array
+// (otherwise xb == xh). ksteps: the K steps of 16 the MMA issues.
 struct TcBuffers {
     void* xh;
+    void* xb;
     float* xr;
     float* cn;
     unsigned* ix;
     void* scale;
     int Kp;
     int dr;
+    int split;
+    int ksteps;
 };
 size_t tc_buffer_bytes(int64_t padded, int d);
 // minmax: the per-dimension (min, max) keys of the spatial-order pass.
@@ -58,7 +67,11 @@ void tc_seed(const TcBuffers& b, int t0, int mt, int d, int k, uint64_t* seed_ke
              cudaStream_t s);
 // Workspace of the per-row lists of one sweep launch batch.
 size_t tc_list_bytes(int nt, int nsplit);
+// qs: the seed window (spiral positions 0..qs-1 are the seed's); plist /
+// pcount (nullable): per row tile, the column tiles to visit in order (the
+// small-d prune lists); without them every tile past the window is visited.
 void tc_sweep(const TcBuffers& b, int nt, int t0, int mt, int nsplit, int d, int k, const unsigned* maxn,
-              unsigned long long* kth_shared, uint64_t* partial, uint64_t* lists, int* status, cudaStream_t s);
+              unsigned long long* kth_shared, uint64_t* partial, uint64_t* lists, int* status, cudaStream_t s,
+              int qs = 1, const uint2* plist = nullptr, const int* pcount = nullptr);
 
 }  // namespace culof_gb300

@@ -37,6 +37,8 @@
 // then rescored exactly.
 #include <cuda_fp16.h>
 
+#include <cstdlib>
+
 #include "common.cuh"
 #include "engine.cuh"
 #include "fast.cuh"
@@ -96,11 +98,14 @@ __global__ void tc_scale_kernel(const unsigned* __restrict__ mm, int d, TcScale*
 
 // Sorted position p: f16 operand row (scaled), FP32 coordinates (row-major,
 // dr = d rounded up to 4, zero padded), norm (+inf for padding) and original
-// index (kNoIndex for padding).
+// index (kNoIndex for padding). With split, element f < 3d of the row
+// operand xh is [hi, lo, hi][f / d] of coordinate f % d and of the column
+// operand xb [hi, hi, lo][f / d]; hi = f16(x), lo = f16(x - hi) (x - hi is
+// exact in float32).
 __global__ void tc_build_kernel(const float* __restrict__ xc, const float* __restrict__ norms, int64_t n, int d,
-                                int Kp, int dr, const unsigned* __restrict__ perm, int64_t padded,
-                                const TcScale* __restrict__ scale, __half* __restrict__ xh, float* __restrict__ xr,
-                                float* __restrict__ cn, unsigned* __restrict__ ix) {
+                                int Kp, int dr, int split, const unsigned* __restrict__ perm, int64_t padded,
+                                const TcScale* __restrict__ scale, __half* __restrict__ xh, __half* __restrict__ xb,
+                                float* __restrict__ xr, float* __restrict__ cn, unsigned* __restrict__ ix) {
     const float sc = scale->sc;
     const int64_t total = padded * Kp;
     for (int64_t e = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; e < total;
@@ -109,9 +114,18 @@ __global__ void tc_build_kernel(const float* __restrict__ xc, const float* __res
         const int f = static_cast<int>(e % Kp);
         const bool valid = p < n;
         const unsigned orig = valid ? perm[p] : kNoIndex;
-        const float x = (valid && f < d) ? xc[static_cast<int64_t>(orig) * d + f] : 0.0f;
-        xh[e] = __float2half_rn(x * sc);
-        if (f < dr) xr[p * dr + f] = x;
+        const int seg = split ? f / d : 0, j = split ? f % d : f;
+        const float x = (valid && j < d && seg < 3) ? xc[static_cast<int64_t>(orig) * d + j] : 0.0f;
+        const float xs = x * sc;
+        const __half hi = __float2half_rn(xs);
+        if (split) {
+            const __half lo = __float2half_rn(__fsub_rn(xs, __half2float(hi)));
+            xh[e] = seg == 1 ? lo : hi;
+            xb[e] = seg == 2 ? lo : hi;
+        } else {
+            xh[e] = hi;
+        }
+        if (f < dr) xr[p * dr + f] = f < d && valid ? xc[static_cast<int64_t>(orig) * d + f] : 0.0f;
         if (f == 0) {
             cn[p] = valid ? norms[orig] : __int_as_float(0x7f800000);
             ix[p] = orig;
@@ -192,20 +206,34 @@ __global__ void __launch_bounds__(256) tc_seed_kernel(const float* __restrict__ 
 //    f_b > thr(fk) = fk + 2 m0 + 2 dl / (1 - dl) max(0, fk + na / (1 - g) + m0)
 //    (+ slack) is strictly farther than every column c with f_c <= fk, so once
 //    k columns with f <= fk are known, b can never be among the k nearest.
+// With split operands (x = hi + r exactly, lo = f16(r), |r| <= uh |x|,
+// |lo - r| <= uh |r| + eta) the summed products hi.hi + lo.hi + hi.lo miss
+// a.b by at most
+//   E = (3 uh^2 + 3 uh^3) A B + eta (1 + uh) sqrt(d) (A + B) + 2 d eta^2
+//       + Ka ua (1 + 3 uh) ((1 + uh) A + sqrt(Ka) eta) ((1 + uh) B + sqrt(Ka) eta)
+// (Ka = the accumulated K, 16 per MMA step), in place of the first line of E.
 struct RowBounds {
     float c0, c3, c4;  // per row: exact offset; approximate offset and shift
 };
 constexpr double kU = 5.9604644775390625e-08;  // 2^-24
 
-__device__ RowBounds row_bounds(float na_f, float nmax_f, int K, float eta_f) {
+__device__ RowBounds row_bounds(float na_f, float nmax_f, int K, float eta_f, int split_d, int kacc) {
     const double uh = 4.8828125e-04;        // 2^-11
     const double ua = 9.5367431640625e-07;  // 2^-20
     const double g = (K + 1) * kU / (1.0 - (K + 1) * kU);
     const double a = static_cast<double>(na_f), m = static_cast<double>(nmax_f), eta = static_cast<double>(eta_f);
     const double A = sqrt(a / (1.0 - g)), B = sqrt(m / (1.0 - g));
-    const double sk = sqrt(static_cast<double>(K));
-    const double E = (2.0 * uh + uh * uh) * A * B + eta * (1.0 + uh) * sk * (A + B) + K * eta * eta +
-                     K * ua * ((1.0 + uh) * A + sk * eta) * ((1.0 + uh) * B + sk * eta);
+    double E;
+    if (split_d > 0) {
+        const double sd = sqrt(static_cast<double>(split_d)), sa = sqrt(static_cast<double>(kacc));
+        E = (3.0 * uh * uh + 3.0 * uh * uh * uh) * A * B + eta * (1.0 + uh) * sd * (A + B) +
+            2.0 * split_d * eta * eta +
+            kacc * ua * (1.0 + 3.0 * uh) * ((1.0 + uh) * A + sa * eta) * ((1.0 + uh) * B + sa * eta);
+    } else {
+        const double sk = sqrt(static_cast<double>(K));
+        E = (2.0 * uh + uh * uh) * A * B + eta * (1.0 + uh) * sk * (A + B) + K * eta * eta +
+            K * ua * ((1.0 + uh) * A + sk * eta) * ((1.0 + uh) * B + sk * eta);
+    }
     const double m0 = g / (1.0 - g) * m + 2.0 * E + kU * (m + 2.0 * (A * B + E));
     const double slack = 8.0 * kU * (a + m + 2.0 * A * B) + 1e-30;
     RowBounds r;
@@ -557,20 +585,30 @@ __noinline__ __device__ void rescore_final(uint64_t* __restrict__ lst, int r, in
 }
 
 __global__ void __launch_bounds__(kTcThreads, 2)
-tc_sweep_kernel(const __grid_constant__ CUtensorMap tmap, const float* __restrict__ xr,
+tc_sweep_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ CUtensorMap tmapb,
+                const float* __restrict__ xr,
                 const float* __restrict__ cn, const unsigned* __restrict__ ix, const TcScale* __restrict__ scale,
-                int nt, int T0, int ntb, int nsplit, int d, int dr, int Kp, int k,
+                int nt, int T0, int ntb, int nsplit, int d, int dr, int Kp, int split_ops, int ksteps, int k,
                 const unsigned* __restrict__ max_norm_bits, unsigned long long* __restrict__ kth_shared,
-                uint64_t* __restrict__ partial, uint64_t* __restrict__ lists, int* __restrict__ status) {
+                uint64_t* __restrict__ partial, uint64_t* __restrict__ lists, int* __restrict__ status, int qs,
+                const uint2* __restrict__ plist, const int* __restrict__ pcount) {
     extern __shared__ uint8_t tc_raw[];
     TcSmem& sh = *reinterpret_cast<TcSmem*>((reinterpret_cast<uintptr_t>(tc_raw) + 1023) & ~uintptr_t(1023));
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int T = T0 + static_cast<int>(blockIdx.x) % ntb;
     const int split = static_cast<int>(blockIdx.x) / ntb;
-    const int per = (nt - 1 + nsplit - 1) / nsplit;
-    const int q0 = 1 + split * per;
+    // the split's column tiles: entries split + nsplit j of the row tile's
+    // prune list (visiting order, tiles that the seed's k-th distances cannot
+    // rule out), or its contiguous share of the spiral past the seed window
+    const int per = (nt - qs + nsplit - 1) / nsplit;
+    const int q0 = qs + split * per;
     const int q1 = min(nt, q0 + per);
-    const int count = q1 > q0 ? q1 - q0 : 0;
+    const int lcount = plist ? pcount[T] : 0;
+    const int count = plist ? (lcount > split ? (lcount - split + nsplit - 1) / nsplit : 0) : (q1 > q0 ? q1 - q0 : 0);
+    const uint2* tlist = plist ? plist + static_cast<int64_t>(T) * nt : nullptr;
+    auto col_tile = [&](int j) -> int {
+        return tlist ? static_cast<int>(tlist[split + nsplit * j].x) : spiral_tile(T, q0 + j, nt);
+    };
     const int nkb = Kp / 64;
     const float nmax = __uint_as_float(*max_norm_bits);
     const int64_t rbase = static_cast<int64_t>(T) * kRT;
@@ -619,9 +657,9 @@ tc_sweep_kernel(const __grid_constant__ CUtensorMap tmap, const float* __restric
                     break;
                 }
                 if (tc_aborted(sh)) break;
-                const int col0 = spiral_tile(T, q0 + j, nt) * kCT;
+                const int col0 = col_tile(j) * kCT;
                 mbar_expect_tx(&sh.full[s], nkb * kBox);
-                for (int kb = 0; kb < nkb; ++kb) tc::tma_load_2d(sh.b[s][kb], &tmap, 64 * kb, col0, &sh.full[s]);
+                for (int kb = 0; kb < nkb; ++kb) tc::tma_load_2d(sh.b[s][kb], &tmapb, 64 * kb, col0, &sh.full[s]);
                 issued = j + 1;
             }
             // no copy may still be landing in shared memory when the CTA exits
@@ -645,7 +683,7 @@ tc_sweep_kernel(const __grid_constant__ CUtensorMap tmap, const float* __restric
                 }
                 tc::tc_fence_after();
                 const uint32_t dt = tmem + static_cast<uint32_t>(acc * 128);
-                for (int kk = 0; kk < 4 * nkb; ++kk) {
+                for (int kk = 0; kk < ksteps; ++kk) {
                     const int kb = kk >> 2, sub = kk & 3;
                     const uint64_t ad = tc::sw128_desc(smem_u32(sh.a[kb]) + 32 * sub);
                     const uint64_t bd = tc::sw128_desc(smem_u32(sh.b[s][kb]) + 32 * sub);
@@ -668,7 +706,7 @@ tc_sweep_kernel(const __grid_constant__ CUtensorMap tmap, const float* __restric
         const TcScale sc = *scale;
         const bool all = sc.all != 0.0f;
         const bool row_valid = __ldg(ix + rbase + r) != kNoIndex;
-        const RowBounds rb = row_bounds(sh.row_norm[r], nmax, Kp, sc.eta);
+        const RowBounds rb = row_bounds(sh.row_norm[r], nmax, Kp, sc.eta, split_ops ? d : 0, 16 * ksteps);
         const float c1 = exact_c1(Kp), c2 = approx_c2(Kp);
         auto row_tau = [&]() -> float {
             if (!row_valid) return __int_as_float(0xff800000);
@@ -682,7 +720,7 @@ tc_sweep_kernel(const __grid_constant__ CUtensorMap tmap, const float* __restric
         // This tile's column norms are staged in a per-warp shared ring one
         // tile ahead (one coalesced 512-byte load per warp), so the filter
         // never waits on global memory.
-        auto tile_base = [&](int jj) -> int64_t { return static_cast<int64_t>(spiral_tile(T, q0 + jj, nt)) * kCT; };
+        auto tile_base = [&](int jj) -> int64_t { return static_cast<int64_t>(col_tile(jj)) * kCT; };
         float4 npre = make_float4(0.f, 0.f, 0.f, 0.f);
         if (count > 0) npre = __ldg(reinterpret_cast<const float4*>(cn + tile_base(0)) + lane);
         int qc = 0;
@@ -837,12 +875,25 @@ tc_sweep_kernel(const __grid_constant__ CUtensorMap tmap, const float* __restric
 
 }  // namespace
 
+// Split operands when the three d-wide segments fit one or two 64-wide
+// boxes (d <= 42). CULOF_TC_SPLIT=0 keeps single f16 operands (measurement).
+static bool tc_use_split(int d) {
+    const char* env = std::getenv("CULOF_TC_SPLIT");
+    if (env && env[0] == '0') return false;
+    return 3 * d <= 128;
+}
+static int tc_kp(int d, bool split) {
+    const int w = split ? 3 * d : d;
+    return w <= 64 ? 64 : 128;
+}
+
 size_t tc_buffer_bytes(int64_t padded, int d) {
-    const int Kp = d <= 64 ? 64 : 128;
+    const bool split = tc_use_split(d);
+    const int Kp = tc_kp(d, split);
     const int dr = (d + 3) & ~3;
     const auto up = [](size_t x) { return (x + 255) & ~static_cast<size_t>(255); };
-    return up(sizeof(__half) * padded * Kp) + up(sizeof(float) * padded * dr) + up(sizeof(float) * padded) +
-           up(sizeof(unsigned) * padded) + up(sizeof(TcScale));
+    return up(sizeof(__half) * padded * Kp) * (split ? 2 : 1) + up(sizeof(float) * padded * dr) +
+           up(sizeof(float) * padded) + up(sizeof(unsigned) * padded) + up(sizeof(TcScale));
 }
 
 size_t tc_list_bytes(int nt, int nsplit) {
@@ -856,11 +907,19 @@ TcBuffers tc_prepare(void* buf, const float* xc, const float* norms, int64_t n, 
     const int64_t padded = static_cast<int64_t>(nt) * kCT;
     const auto up = [](size_t x) { return (x + 255) & ~static_cast<size_t>(255); };
     TcBuffers b;
-    b.Kp = d <= 64 ? 64 : 128;
+    const bool split = tc_use_split(d);
+    b.split = split ? 1 : 0;
+    b.Kp = tc_kp(d, split);
+    b.ksteps = split ? (3 * d + 15) / 16 : b.Kp / 16;
     b.dr = (d + 3) & ~3;
     char* p = static_cast<char*>(buf);
     b.xh = p;
     p += up(sizeof(__half) * padded * b.Kp);
+    b.xb = b.xh;
+    if (split) {
+        b.xb = p;
+        p += up(sizeof(__half) * padded * b.Kp);
+    }
     b.xr = reinterpret_cast<float*>(p);
     p += up(sizeof(float) * padded * b.dr);
     b.cn = reinterpret_cast<float*>(p);
@@ -872,9 +931,10 @@ TcBuffers tc_prepare(void* buf, const float* xc, const float* norms, int64_t n, 
     CG_LAUNCH_CHECK();
     int64_t g = ceil_div(padded * b.Kp, 256);
     if (g > 152 * 16) g = 152 * 16;
-    tc_build_kernel<<<static_cast<unsigned>(g), 256, 0, s>>>(xc, norms, n, d, b.Kp, b.dr, perm, padded,
+    tc_build_kernel<<<static_cast<unsigned>(g), 256, 0, s>>>(xc, norms, n, d, b.Kp, b.dr, b.split, perm, padded,
                                                              reinterpret_cast<const TcScale*>(b.scale),
-                                                             static_cast<__half*>(b.xh), b.xr, b.cn, b.ix);
+                                                             static_cast<__half*>(b.xh), static_cast<__half*>(b.xb),
+                                                             b.xr, b.cn, b.ix);
     CG_LAUNCH_CHECK();
     return b;
 }
@@ -888,18 +948,20 @@ void tc_seed(const TcBuffers& b, int t0, int mt, int d, int k, uint64_t* seed_ke
 }
 
 void tc_sweep(const TcBuffers& b, int nt, int t0, int mt, int nsplit, int d, int k, const unsigned* maxn,
-              unsigned long long* kth_shared, uint64_t* partial, uint64_t* lists, int* status, cudaStream_t s) {
+              unsigned long long* kth_shared, uint64_t* partial, uint64_t* lists, int* status, cudaStream_t s, int qs,
+              const uint2* plist, const int* pcount) {
     const size_t smem = sizeof(TcSmem) + 1024;
     set_max_dynamic_smem(reinterpret_cast<const void*>(tc_sweep_kernel), static_cast<int>(smem));
     const CUtensorMap map = tc::make_kmajor_map(b.xh, static_cast<int64_t>(nt) * kCT, b.Kp, true);
+    const CUtensorMap mapb = tc::make_kmajor_map(b.xb, static_cast<int64_t>(nt) * kCT, b.Kp, true);
     // row tiles in batches, so that the list workspace stays bounded
     const int ntb_max = kTcMaxCtasPerLaunch / nsplit > 0 ? kTcMaxCtasPerLaunch / nsplit : 1;
     for (int T0 = t0; T0 < t0 + mt; T0 += ntb_max) {
         const int ntb = t0 + mt - T0 < ntb_max ? t0 + mt - T0 : ntb_max;
-        tc_sweep_kernel<<<ntb * nsplit, kTcThreads, smem, s>>>(map, b.xr, b.cn, b.ix,
+        tc_sweep_kernel<<<ntb * nsplit, kTcThreads, smem, s>>>(map, mapb, b.xr, b.cn, b.ix,
                                                                reinterpret_cast<const TcScale*>(b.scale), nt, T0, ntb,
-                                                               nsplit, d, b.dr, b.Kp, k, maxn, kth_shared, partial,
-                                                               lists, status);
+                                                               nsplit, d, b.dr, b.Kp, b.split, b.ksteps, k, maxn,
+                                                               kth_shared, partial, lists, status, qs, plist, pcount);
         CG_LAUNCH_CHECK();
     }
 }
