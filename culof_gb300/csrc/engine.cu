@@ -153,15 +153,21 @@ int Engine::choose_path(int64_t n, int d, int k) const {
         throw Error(kInvalidArgument, "fused path requested but unsupported for this n/d/k");
     if (p == kPathFast || p == kPathTensor) return p;
     if (!ok || n <= kSmallN) return kPathGeneral;
-    if (d <= 8) return kPathFast;
-    // 8 < d <= 16 with fewer row tiles than one wave of tensor CTAs (two per
-    // SM): the FP32 wide sweep is as fast or faster on every input measured
-    // (n = 20k: 1.8 ms against 1.85-2.8 ms on clustered, mixture and
-    // low-rank data); beyond that the tensor path wins or ties
+    // d <= 8: the FP32 small-d sweep up to k = 48; above it the tensor sweep
+    // (split f16 operands over the same seed window and prune lists) wins
+    // (fit_predict on clusters, k = 64: n = 20k, 3.3 against 5.4 ms;
+    // n = 200k, 25.5 against 50.1 ms; at k = 48 the FP32 sweep is ahead or
+    // level: 2.3 / 3.2 / 19.0 against 2.4 / 4.8 / 19.1 ms at 20k / 50k / 200k)
+    if (d <= 8) return k > 48 ? kPathTensor : kPathFast;
+    // 8 < d <= 16 with fewer row tiles than SMs: the FP32 wide sweep ties the
+    // tensor path (n = 20k, d = 16: 1.91 against 1.87 ms); from there up the
+    // tensor path wins (n = 30k: 2.33 against 2.80 ms; 38k: 3.01 against
+    // 3.79 ms), and at every size for d > 16 (d = 24, n = 20k: 1.81 against
+    // 2.31 ms; d = 32, n = 10k: 1.15 against 1.45 ms)
     int sms = 0;
     CG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_));
     const int64_t nt = (n + 127) / 128;
-    if (d <= 16 && nt < 2 * static_cast<int64_t>(sms)) return kPathFast;
+    if (d <= 16 && nt < static_cast<int64_t>(sms)) return kPathFast;
     return kPathTensor;
 }
 
