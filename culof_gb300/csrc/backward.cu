@@ -33,37 +33,52 @@ __device__ __forceinline__ void flag_bad(int* status) { atomicExch(status, 2); }
 // gradient, never an out-of-range access.
 __device__ __forceinline__ int64_t clampj(int32_t j, int64_t n) { return j < 0 ? 0 : (j >= n ? n - 1 : j); }
 
+// The per-point sums below run one warp per point: lanes take the terms
+// lane, lane + 32, ... in order and a fixed xor-shuffle tree adds the lanes'
+// partials, so every sum has one fixed order and the gradient is
+// bit-reproducible.
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = __dadd_rn(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ int64_t warp_id() { return (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; }
+__device__ __forceinline__ int64_t warp_count() { return (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5; }
+
 // d2[e] (e = t * n + i, the layout of the k-NN slots) in FP64 from the raw
-// points: (x_i - x_j) * inv_std, the mean cancels.
+// points: (x_i - x_j) * inv_std, the mean cancels. A warp per point, lanes
+// over dimensions.
 __global__ void bw_pair_kernel(const float* __restrict__ x, int64_t n, int d, int k, const int32_t* __restrict__ nbr,
                                const double* __restrict__ inv, double* __restrict__ d2, int* __restrict__ status) {
-    const int64_t total = n * k;
-    for (int64_t e = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; e < total;
-         e += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-        const int64_t i = e % n;
-        const int32_t j = nbr[e];
-        double s = 0.0;
-        if (j < 0 || j >= n) {
-            flag_bad(status);
-        } else {
-            const float* xi = x + i * d;
-            const float* xj = x + static_cast<int64_t>(j) * d;
-            for (int f = 0; f < d; ++f) {
-                const double t = __dmul_rn(__dsub_rn(static_cast<double>(xi[f]), static_cast<double>(xj[f])), inv[f]);
-                s = __fma_rn(t, t, s);
+    const int lane = threadIdx.x & 31;
+    for (int64_t i = warp_id(); i < n; i += warp_count()) {
+        const float* xi = x + i * d;
+        for (int t = 0; t < k; ++t) {
+            const int64_t e = static_cast<int64_t>(t) * n + i;
+            const int32_t j = nbr[e];
+            double s = 0.0;
+            if (j < 0 || j >= n) {
+                if (lane == 0) flag_bad(status);
+            } else {
+                const float* xj = x + static_cast<int64_t>(j) * d;
+                for (int f = lane; f < d; f += 32) {
+                    const double u = __dmul_rn(__dsub_rn(static_cast<double>(xi[f]), static_cast<double>(xj[f])), inv[f]);
+                    s = __fma_rn(u, u, s);
+                }
             }
+            s = warp_sum(s);
+            if (lane == 0) d2[e] = s;
         }
-        d2[e] = s;
     }
 }
 
-// Per point: reach distances of its slots, lrd.
+// Per point: reach distances of its slots, lrd. A warp per point, lanes over slots.
 __global__ void bw_lrd_kernel(int64_t n, int k, const int32_t* __restrict__ nbr, const double* __restrict__ d2,
                               double* __restrict__ reach, double* __restrict__ lrd) {
-    for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
-         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int lane = threadIdx.x & 31;
+    for (int64_t i = warp_id(); i < n; i += warp_count()) {
         double R = 0.0;
-        for (int t = 0; t < k; ++t) {
+        for (int t = lane; t < k; t += 32) {
             const int64_t e = static_cast<int64_t>(t) * n + i;
             const int64_t j = clampj(nbr[e], n);
             const double kd = d2[static_cast<int64_t>(k - 1) * n + j];
@@ -71,19 +86,23 @@ __global__ void bw_lrd_kernel(int64_t n, int k, const int32_t* __restrict__ nbr,
             reach[e] = r;
             R = __dadd_rn(R, r);
         }
-        lrd[i] = __ddiv_rn(1.0, __dadd_rn(__ddiv_rn(R, static_cast<double>(k)), 1e-10));
+        R = warp_sum(R);
+        if (lane == 0) lrd[i] = __ddiv_rn(1.0, __dadd_rn(__ddiv_rn(R, static_cast<double>(k)), 1e-10));
     }
 }
 
-// Per point: S_i = sum_j lrd_j and the score.
+// Per point: S_i = sum_j lrd_j and the score. A warp per point.
 __global__ void bw_score_kernel(int64_t n, int k, const int32_t* __restrict__ nbr, const double* __restrict__ lrd,
                                 double* __restrict__ S, double* __restrict__ score) {
-    for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
-         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int lane = threadIdx.x & 31;
+    for (int64_t i = warp_id(); i < n; i += warp_count()) {
         double s = 0.0;
-        for (int t = 0; t < k; ++t) s = __dadd_rn(s, lrd[clampj(nbr[static_cast<int64_t>(t) * n + i], n)]);
-        S[i] = s;
-        if (score) score[i] = __ddiv_rn(s, __dmul_rn(static_cast<double>(k), lrd[i]));
+        for (int t = lane; t < k; t += 32) s = __dadd_rn(s, lrd[clampj(nbr[static_cast<int64_t>(t) * n + i], n)]);
+        s = warp_sum(s);
+        if (lane == 0) {
+            S[i] = s;
+            if (score) score[i] = __ddiv_rn(s, __dmul_rn(static_cast<double>(k), lrd[i]));
+        }
     }
 }
 
@@ -101,19 +120,23 @@ __global__ void bw_rev_init_kernel(int64_t n, int64_t total, const int32_t* __re
 }
 
 // dL/dlrd_m = -g_m S_m / (k lrd_m^2) + sum over reverse slots (i, t) of g_i / (k lrd_i).
+// (A warp per point, lanes over the reverse slots.)
 __global__ void bw_glrd_kernel(int64_t n, int k, const double* __restrict__ g, const double* __restrict__ lrd,
                                const double* __restrict__ S, const unsigned* __restrict__ off,
                                const unsigned* __restrict__ rev, double* __restrict__ glrd) {
     const double dk = static_cast<double>(k);
-    for (int64_t m = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; m < n;
-         m += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-        const double lm = lrd[m];
-        double acc = -__ddiv_rn(__dmul_rn(g[m], S[m]), __dmul_rn(dk, __dmul_rn(lm, lm)));
-        for (unsigned p = off[m]; p < off[m + 1]; ++p) {
+    const int lane = threadIdx.x & 31;
+    for (int64_t m = warp_id(); m < n; m += warp_count()) {
+        double acc = 0.0;
+        for (unsigned p = off[m] + lane; p < off[m + 1]; p += 32) {
             const int64_t i = static_cast<int64_t>(rev[p]) % n;
             acc = __dadd_rn(acc, __ddiv_rn(g[i], __dmul_rn(dk, lrd[i])));
         }
-        glrd[m] = acc;
+        acc = warp_sum(acc);
+        if (lane == 0) {
+            const double lm = lrd[m];
+            glrd[m] = __dadd_rn(-__ddiv_rn(__dmul_rn(g[m], S[m]), __dmul_rn(dk, __dmul_rn(lm, lm))), acc);
+        }
     }
 }
 
@@ -141,14 +164,18 @@ __global__ void bw_route_kernel(int64_t n, int k, const int32_t* __restrict__ nb
 
 // Per point j: the k-distance gradient (sum over its reverse slots, fixed
 // order) joins the gradient of its own slot k-1.
+// (A warp per point.)
 __global__ void bw_kd_kernel(int64_t n, int k, const unsigned* __restrict__ off, const unsigned* __restrict__ rev,
                              const double* __restrict__ gkd, double* __restrict__ gd2) {
-    for (int64_t j = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; j < n;
-         j += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int lane = threadIdx.x & 31;
+    for (int64_t j = warp_id(); j < n; j += warp_count()) {
         double s = 0.0;
-        for (unsigned p = off[j]; p < off[j + 1]; ++p) s = __dadd_rn(s, gkd[rev[p]]);
-        const int64_t e = static_cast<int64_t>(k - 1) * n + j;
-        gd2[e] = __dadd_rn(gd2[e], s);
+        for (unsigned p = off[j] + lane; p < off[j + 1]; p += 32) s = __dadd_rn(s, gkd[rev[p]]);
+        s = warp_sum(s);
+        if (lane == 0) {
+            const int64_t e = static_cast<int64_t>(k - 1) * n + j;
+            gd2[e] = __dadd_rn(gd2[e], s);
+        }
     }
 }
 
@@ -192,47 +219,80 @@ __global__ void bw_gx_kernel(const float* __restrict__ x, int64_t n, int d, int 
 }
 
 // Per (chunk of kCenterChunk rows, feature): partial sums of gxc and of
-// gxc * xc, summed in row order; then per feature in chunk order.
-__global__ void bw_col_partials_kernel(const float* __restrict__ x, int64_t n, int d, const double* __restrict__ mean,
-                                       const double* __restrict__ inv, const double* __restrict__ gxc,
-                                       double* __restrict__ pa, double* __restrict__ pb) {
+// gxc * xc; then per feature over the chunks. One block per chunk: warp w
+// sums rows w, w + 8, ... of the chunk in order (lanes over features), and
+// the 8 warps' partials are added in warp order.
+constexpr int kColMaxD = 128;
+__global__ void __launch_bounds__(256) bw_col_partials_kernel(const float* __restrict__ x, int64_t n, int d,
+                                                              const double* __restrict__ mean,
+                                                              const double* __restrict__ inv,
+                                                              const double* __restrict__ gxc,
+                                                              double* __restrict__ pa, double* __restrict__ pb) {
+    __shared__ double sa[8][kColMaxD], sb[8][kColMaxD];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int64_t chunks = ceil_div(n, kCenterChunk);
-    for (int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; t < chunks * d;
-         t += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-        const int64_t c = t / d;
-        const int f = static_cast<int>(t % d);
-        double a = 0.0, b = 0.0;
+    for (int64_t c = blockIdx.x; c < chunks; c += gridDim.x) {
         const int64_t r1 = (c + 1) * kCenterChunk < n ? (c + 1) * kCenterChunk : n;
-        for (int64_t r = c * kCenterChunk; r < r1; ++r) {
-            const double g = gxc[r * d + f];
-            const double xc = __dmul_rn(__dsub_rn(static_cast<double>(x[r * d + f]), mean[f]), inv[f]);
-            a = __dadd_rn(a, g);
-            b = __fma_rn(g, xc, b);
+        for (int fb = 0; fb < d; fb += kColMaxD) {  // blocks of features that fit the shared arrays
+            const int fe = d - fb < kColMaxD ? d - fb : kColMaxD;
+            for (int f0 = 0; f0 < fe; f0 += 32) {
+                const int fl = f0 + lane, f = fb + fl;
+                if (fl < fe) {
+                    double a = 0.0, b = 0.0;
+                    const double mf = mean[f], vf = inv[f];
+                    for (int64_t r = c * kCenterChunk + warp; r < r1; r += 8) {
+                        const double g = gxc[r * d + f];
+                        const double xc = __dmul_rn(__dsub_rn(static_cast<double>(x[r * d + f]), mf), vf);
+                        a = __dadd_rn(a, g);
+                        b = __fma_rn(g, xc, b);
+                    }
+                    sa[warp][fl] = a;
+                    sb[warp][fl] = b;
+                }
+            }
+            __syncthreads();
+            for (int fl = threadIdx.x; fl < fe; fl += blockDim.x) {
+                double a = 0.0, b = 0.0;
+                for (int w = 0; w < 8; ++w) {
+                    a = __dadd_rn(a, sa[w][fl]);
+                    b = __dadd_rn(b, sb[w][fl]);
+                }
+                pa[c * d + fb + fl] = a;
+                pb[c * d + fb + fl] = b;
+            }
+            __syncthreads();
         }
-        pa[t] = a;
-        pb[t] = b;
     }
 }
 
 // Per feature: column means A_f = mean(gxc), B_f = mean(gxc * xc) and whether
 // the feature was scaled (normalising and std > 1e-12, the rule of the
 // forward centring).
+// (A warp per feature, lanes over the chunks; the variance partials are
+// summed in chunk order, as the forward centring sums them.)
 __global__ void bw_col_finalize_kernel(int64_t n, int d, int normalize, const double* __restrict__ pa,
                                        const double* __restrict__ pb, const double* __restrict__ var_partial,
                                        double* __restrict__ A, double* __restrict__ B, int* __restrict__ scaled) {
-    const int f = blockIdx.x * blockDim.x + threadIdx.x;
-    if (f >= d) return;
+    const int lane = threadIdx.x & 31;
     const int64_t chunks = ceil_div(n, kCenterChunk);
     const double dn = static_cast<double>(n);
-    double a = 0.0, b = 0.0, v = 0.0;
-    for (int64_t c = 0; c < chunks; ++c) {
-        a = __dadd_rn(a, pa[c * d + f]);
-        b = __dadd_rn(b, pb[c * d + f]);
-        if (normalize) v = __dadd_rn(v, var_partial[c * d + f]);
+    for (int64_t f = warp_id(); f < d; f += warp_count()) {
+        double a = 0.0, b = 0.0;
+        for (int64_t c = lane; c < chunks; c += 32) {
+            a = __dadd_rn(a, pa[c * d + f]);
+            b = __dadd_rn(b, pb[c * d + f]);
+        }
+        a = warp_sum(a);
+        b = warp_sum(b);
+        if (lane == 0) {
+            double v = 0.0;
+            if (normalize)
+                for (int64_t c = 0; c < chunks; ++c) v = __dadd_rn(v, var_partial[c * d + f]);
+            A[f] = __ddiv_rn(a, dn);
+            B[f] = __ddiv_rn(b, dn);
+            scaled[f] = normalize && __dsqrt_rn(__ddiv_rn(v, dn)) > 1e-12;
+        }
     }
-    A[f] = __ddiv_rn(a, dn);
-    B[f] = __ddiv_rn(b, dn);
-    scaled[f] = normalize && __dsqrt_rn(__ddiv_rn(v, dn)) > 1e-12;
 }
 
 // dL/dx: centring (and scaling) backward of the normalised-coordinate gradient.
@@ -314,11 +374,11 @@ void Engine::lof_backward_device(const float* d_x, int64_t n, int d, int k, bool
     int* status = status_ptr();
     double* score = scores_out;
 
-    bw_pair_kernel<<<grid_of(total), 256, 0, s>>>(d_x, n, d, k, nbr_idx, inv, d2, status);
+    bw_pair_kernel<<<grid_of(n * 32), 256, 0, s>>>(d_x, n, d, k, nbr_idx, inv, d2, status);
     CG_LAUNCH_CHECK();
-    bw_lrd_kernel<<<grid_of(n), 256, 0, s>>>(n, k, nbr_idx, d2, reach, lrd);
+    bw_lrd_kernel<<<grid_of(n * 32), 256, 0, s>>>(n, k, nbr_idx, d2, reach, lrd);
     CG_LAUNCH_CHECK();
-    bw_score_kernel<<<grid_of(n), 256, 0, s>>>(n, k, nbr_idx, lrd, S, score);
+    bw_score_kernel<<<grid_of(n * 32), 256, 0, s>>>(n, k, nbr_idx, lrd, S, score);
     CG_LAUNCH_CHECK();
     // transposed slots: offsets from the per-index counts, slots in (t, i)
     // enumeration order within each index (stable sort)
@@ -331,20 +391,22 @@ void Engine::lof_backward_device(const float* d_x, int64_t n, int d, int k, bool
     unsigned* rev = nullptr;
     sort_pairs_stable(keys, vals, keys2, vals2, total, bits, counts, s, &rev);
 
-    bw_glrd_kernel<<<grid_of(n), 256, 0, s>>>(n, k, grad_scores, lrd, S, off, rev, glrd);
+    bw_glrd_kernel<<<grid_of(n * 32), 256, 0, s>>>(n, k, grad_scores, lrd, S, off, rev, glrd);
     CG_LAUNCH_CHECK();
     bw_route_kernel<<<grid_of(total), 256, 0, s>>>(n, k, nbr_idx, d2, reach, lrd, glrd, gd2, gkd);
     CG_LAUNCH_CHECK();
-    bw_kd_kernel<<<grid_of(n), 256, 0, s>>>(n, k, off, rev, gkd, gd2);
+    bw_kd_kernel<<<grid_of(n * 32), 256, 0, s>>>(n, k, off, rev, gkd, gd2);
     CG_LAUNCH_CHECK();
     bw_gx_kernel<<<grid_of(n * 32), 256, 0, s>>>(d_x, n, d, k, nbr_idx, inv, gd2, off, rev, gxc);
     CG_LAUNCH_CHECK();
     // the centring statistics' partials of (x - mean)^2 are still in `partial`
     // when normalising (the second pass of center())
-    bw_col_partials_kernel<<<grid_of(static_cast<int64_t>(chunks_d)), 256, 0, s>>>(d_x, n, d, mean, inv, gxc, pa, pb);
+    const int64_t col_chunks = ceil_div(n, kCenterChunk);
+    bw_col_partials_kernel<<<static_cast<int>(col_chunks < 152 * 8 ? col_chunks : 152 * 8), 256, 0, s>>>(
+        d_x, n, d, mean, inv, gxc, pa, pb);
     CG_LAUNCH_CHECK();
-    bw_col_finalize_kernel<<<static_cast<int>(ceil_div(d, 128)), 128, 0, s>>>(n, d, normalize ? 1 : 0, pa, pb, partial,
-                                                                               A, B, scaled);
+    bw_col_finalize_kernel<<<static_cast<int>(ceil_div(static_cast<int64_t>(d) * 32, 256)), 256, 0, s>>>(
+        n, d, normalize ? 1 : 0, pa, pb, partial, A, B, scaled);
     CG_LAUNCH_CHECK();
     bw_apply_kernel<<<grid_of(n * d), 256, 0, s>>>(d_x, n, d, mean, inv, gxc, A, B, scaled, grad_x);
     CG_LAUNCH_CHECK();

@@ -46,6 +46,8 @@ CASES = [
     ("dups", lambda: np.repeat(np.random.default_rng(56).standard_normal((100, 4)).astype(np.float32), 8,
                                axis=0), 10, False),
     ("d128_k50", lambda: synthetic.factor_model(3000, 128, seed=57), 50, False),
+    # more features than one block of the column reduction (128)
+    ("d200_k10_norm", lambda: synthetic.reference_test_data(1500, 200, seed=61, n_outliers=15), 10, True),
 ]
 
 
