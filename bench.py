@@ -94,6 +94,8 @@ def parse_args():
     p.add_argument("--batched", type=int, default=0, metavar="N",
                    help="the batched problem mix (d = 16, k 10-40, n log-uniform in [128, 16384]) with N problems, "
                         "batched call against single calls")
+    p.add_argument("--autotune-table", action="store_true",
+                   help="the batched autotuner's variant times and choice for a grid of batch layouts")
     p.add_argument("--backward", action="store_true",
                    help="the gradient workload alone (mixture, --n/--d/--k): forward + sparse backward timing")
     p.add_argument("--scaling", action="store_true",
@@ -782,8 +784,38 @@ def run_backward(args):
     return 0
 
 
+def run_autotune_table(args):
+    """The batched autotuner's record per batch layout: the batched problem
+    mix (3 clusters + 2% outliers per problem, n log-uniform in [128, 16384],
+    k in 10..40) with several problem counts and dimensions; one line per
+    layout with every variant's time and the variant chosen."""
+    import torch
+
+    from culof_gb300 import _culof
+
+    torch.cuda.set_device(0)
+    synthetic = load_synthetic()
+    layouts = [(c, d) for d in (4, 8, 16) for c in (64, 256, 2048)] + [(c, d) for d in (32, 64) for c in (64, 256)]
+    for count, d in layouts:
+        probs, ks = synthetic.batched_problems(count, d, seed=0)
+        Xb = np.concatenate(probs).astype(np.float32)
+        offs = np.zeros(len(probs) + 1, np.int64)
+        offs[1:] = np.cumsum([len(p) for p in probs])
+        with _culof.Context() as ctx:
+            dX = torch.from_numpy(Xb).cuda()
+            ds = torch.empty(len(Xb), device="cuda")
+            ctx.lof_batched_device(offs, ks, dX.data_ptr(), d, False, ds.data_ptr())
+            ctx.synchronize()
+            tune = ctx.batched_tuning()
+        print(json.dumps({"problems": count, "points": int(offs[-1]), "d": d, **tune,
+                          "device": _culof.device_info()}), flush=True)
+    return 0
+
+
 def main():
     args = parse_args()
+    if args.autotune_table:
+        return run_autotune_table(args)
     if args.suite:
         return run_suite(args)
     if args.batched:

@@ -78,6 +78,7 @@ _SIGS = {
     "culof_context_lof_backward_device": ([_P, _P, _I64, _I, _I, _I, _P, _P, _P, _P], _I),
     "culof_context_lof_batched_device": ([_P, _I, _P, _P, _P, _I, _I, _P], _I),
     "culof_context_set_graphs": ([_P, _I], _I),
+    "culof_context_batched_tuning": ([_P, _P, ctypes.POINTER(_I), ctypes.POINTER(_I)], _I),
     "culof_lof_batched": ([_I, _P, _P, _P, _I, _I, _P], _I),
     "culof_context_lof_batched": ([_P, _I, _P, _P, _P, _I, _I, _P], _I),
     "culof_context_pair_stats": ([_P, ctypes.POINTER(_D), ctypes.POINTER(_D)], _I),
@@ -348,6 +349,15 @@ class Context:
         """Run a bounded wait that never completes; raises CudaError (the
         failure path of every kernel wait), the context stays usable."""
         _check(_lib.culof_context_probe_bounded_wait(self._h, int(spin_limit)))
+
+    def batched_tuning(self) -> dict:
+        """The batched autotuner's variant times (ms) and choice for the current layout."""
+        ms = np.zeros(4, np.float32)
+        per, pairs = ctypes.c_int(0), ctypes.c_int(0)
+        _check(_lib.culof_context_batched_tuning(self._h, ms.ctypes.data, ctypes.byref(per), ctypes.byref(pairs)))
+        times = {f"{c}cta_{p}pair": float(ms[2 * (c - 1) + (p - 1)]) for c in (1, 2) for p in (1, 2)
+                 if ms[2 * (c - 1) + (p - 1)] >= 0}
+        return {"ms": times, "ctas_per_sm": per.value, "pairs_per_lane": pairs.value}
 
     def set_graphs(self, on: bool) -> None:
         _check(_lib.culof_context_set_graphs(self._h, int(bool(on))))

@@ -327,6 +327,14 @@ int culof_context_set_graphs(culof_context* ctx, int on) {
     return guarded([&] { engine_of(ctx).set_graphs(on != 0); });
 }
 
+int culof_context_batched_tuning(culof_context* ctx, float* ms4, int* ctas_per_sm, int* pairs_per_lane) {
+    return guarded([&] {
+        if (!ms4 || !ctas_per_sm || !pairs_per_lane)
+            throw Error(culof_gb300::kInvalidArgument, "output pointers must not be null");
+        engine_of(ctx).batched_tuning(ms4, ctas_per_sm, pairs_per_lane);
+    });
+}
+
 int culof_context_lof_backward_device(culof_context* ctx, const float* d_points, int64_t n_points, int n_dims, int k,
                                       int normalize, const int32_t* d_nbr_idx, const double* d_grad_scores,
                                       double* d_grad_points, double* d_scores_out) {

@@ -787,6 +787,7 @@ void Engine::batch_autotune(const float* d_x, float* d_scores) {
     CG_CUDA(cudaEventCreate(&e0));
     CG_CUDA(cudaEventCreate(&e1));
     float best = 1e30f;
+    for (float& t : btune_ms_) t = -1.0f;
     for (int per = 1; per <= max_per_sm; ++per) {
         for (int packed = 0; packed <= (dp <= 16 ? 1 : 0); ++packed) {
             btune_grid_ = per * sms;
@@ -798,6 +799,7 @@ void Engine::batch_autotune(const float* d_x, float* d_scores) {
             CG_CUDA(cudaEventSynchronize(e1));
             float ms = 0.0f;
             CG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            btune_ms_[2 * (per - 1) + packed] = ms;
             if (ms < best) {
                 best = ms;
                 bbest_grid_ = btune_grid_;
@@ -874,4 +876,15 @@ void Engine::lof_batched_host(int num, const int64_t* offsets, const int* ks, co
     check_status();
 }
 
+}  // namespace culof_gb300
+
+namespace culof_gb300 {
+void Engine::batched_tuning(float* ms4, int* per_sm, int* pairs_per_lane) const {
+    for (int i = 0; i < 4; ++i) ms4[i] = btuned_ ? btune_ms_[i] : -1.0f;
+    const int sms = bbest_grid_ > 0 ? bbest_grid_ : 1;
+    int dev_sms = 152;
+    cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, device_);
+    *per_sm = btuned_ ? sms / (dev_sms > 0 ? dev_sms : 1) : 0;
+    *pairs_per_lane = btuned_ ? (bbest_packed_ ? 2 : 1) : 0;
+}
 }  // namespace culof_gb300

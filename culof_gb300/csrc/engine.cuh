@@ -112,6 +112,11 @@ public:
     void lof_batched_host(int num, const int64_t* offsets, const int* ks, const float* x, int d, bool normalize,
                           float* scores);
     void set_graphs(bool on) { use_graphs_ = on; }
+    // The batched autotuner's measurements for the current layout (times of
+    // the whole batched call): ms4[2 (c - 1) + (p - 1)] for the k-NN kernel at
+    // c CTAs per SM and p column pairs per lane (-1: not tried), and its
+    // choice (0 before the first batched call).
+    void batched_tuning(float* ms4, int* per_sm, int* pairs_per_lane) const;
     // Pairs the last FP32 small-d sweep evaluated and the pairs of an
     // unpruned sweep (both 0 for other paths); synchronises.
     void pair_stats(double* evaluated, double* total);
@@ -156,6 +161,7 @@ private:
     bool use_graphs_ = true;
     bool btuned_ = false, btune_packed_ = true, bbest_packed_ = true;
     int btune_grid_ = 152, bbest_grid_ = 152;
+    float btune_ms_[4] = {-1.0f, -1.0f, -1.0f, -1.0f};  // (CTAs per SM 1..2) x (column pairs 1..2)
     cudaGraphExec_t bgraph_exec_ = nullptr;
     bool bgraph_valid_ = false;
     const float* bgraph_x_ = nullptr;

@@ -223,6 +223,13 @@ CULOF_API int culof_context_lof_batched(culof_context* ctx, int num_problems, co
                                         const float* points, int n_dims, int normalize, float* scores_out);
 /* Graph capture of repeated batched calls: on (1, default) or off (0). */
 CULOF_API int culof_context_set_graphs(culof_context* ctx, int on);
+/* The batched autotuner's record for the context's current batch layout
+ * (measurement support; no reference counterpart): ms4[2 (c - 1) + (p - 1)]
+ * is the whole batched call's time in milliseconds with the k-NN kernel at
+ * c CTAs per SM and p column pairs per lane (-1 if that variant was not
+ * tried: two CTAs need the shared memory, two pairs d <= 16), and *ctas_per_sm /
+ * *pairs_per_lane the chosen variant (0 before the first batched call). */
+CULOF_API int culof_context_batched_tuning(culof_context* ctx, float* ms4, int* ctas_per_sm, int* pairs_per_lane);
 
 /* Sparse LOF backward (no reference counterpart: the reference has no
  * gradient). Gradient of L = sum_i g_i score_i with respect to the points, the

@@ -135,3 +135,22 @@ def test_package_lof_batched_host_arrays():
         np.testing.assert_array_equal(g, culof_gb300.lof(p, 15))
     with pytest.raises(ValueError):
         culof_gb300.lof_batched(probs[:2], [10])
+
+
+def test_autotuner_record_names_the_fastest_variant():
+    torch = pytest.importorskip("torch")
+    probs, ks = synthetic.batched_problems(48, 16, seed=3)
+    Xb = np.concatenate(probs).astype(np.float32)
+    offs = np.zeros(len(probs) + 1, np.int64)
+    offs[1:] = np.cumsum([len(p) for p in probs])
+    with _culof.Context() as ctx:
+        assert ctx.batched_tuning()["ctas_per_sm"] == 0  # nothing tuned yet
+        dX = torch.from_numpy(Xb).cuda()
+        ds = torch.empty(len(Xb), device="cuda")
+        ctx.lof_batched_device(offs, ks, dX.data_ptr(), 16, False, ds.data_ptr())
+        ctx.synchronize()
+        tune = ctx.batched_tuning()
+    assert tune["ctas_per_sm"] in (1, 2) and tune["pairs_per_lane"] in (1, 2)
+    assert tune["ms"] and all(v > 0 for v in tune["ms"].values())
+    chosen = f"{tune['ctas_per_sm']}cta_{tune['pairs_per_lane']}pair"
+    assert tune["ms"][chosen] == min(tune["ms"].values())
