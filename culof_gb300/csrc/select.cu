@@ -19,6 +19,7 @@
 #include "block.cuh"
 #include "common.cuh"
 #include "prep.cuh"
+#include "warp_sort.cuh"
 
 namespace culof_gb300 {
 
@@ -88,9 +89,11 @@ distance_tile_kernel(const float* __restrict__ xc, int64_t n, int d, int64_t row
 //     built with warp-aggregated shared atomics (lanes with the same bin
 //     elect one adder) locates the bucket of the k-th key; a warp narrows the
 //     bins by ballots over lane prefix sums (4096 -> 128 -> 4 -> 1);
-//   * the keys of that bucket (typically a few hundred) are copied to shared
-//     memory with their columns and sorted (bitonic), which gives the k-th
-//     key; a bucket too large for the buffer is narrowed first by a second
+//   * the keys of that bucket (typically a few dozen) are copied to shared
+//     memory with their columns and sorted, which gives the k-th key: up to
+//     128 keys by one warp in registers (no block barrier), more by the whole
+//     block (bitonic in shared memory); a bucket too large for the buffer is
+//     narrowed first by a second
 //     histogram (bits 18..7) and, if still too large, by a third (bits 6..0),
 //     which pins the k-th key's bits exactly;
 //   * every warp knows how many keys of its segment lie below the k-th key
@@ -118,6 +121,7 @@ struct RowSelect {
     int below;        // keys strictly below the current bucket
     int need;         // rank of the k-th key inside the current bucket (1-based)
     int bucket;       // keys inside the current bucket
+    unsigned kth;     // the k-th key, once found
 };
 
 // Levels of the bucket search: (lowest bit, width). Keys are < 2^31.
@@ -289,8 +293,43 @@ row_select_kernel(float* __restrict__ tile, const float* __restrict__ norms, int
             sh.warp_eq[warp] = 0;
         }
         __syncthreads();
-        // bitonic sort of the bucket, padded to a power of two with ~0
         const int m = sh.ncand;
+        if (m <= 128) {
+            // the usual case: one warp sorts the bucket in registers (a
+            // 128-key bitonic network, element e = lane + 32 j) and counts
+            // its keys below / equal to the k-th by owning warp; no block
+            // barrier until the result is published
+            if (warp == 0) {
+                uint64_t v[4];
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const int e = 32 * j + lane;
+                    v[j] = e < m ? sh.cand[e] : ~0ull;
+                }
+                warp_bitonic_sort<4>(v);
+                const int rk = sh.need - 1;
+                uint64_t kk = 0;
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const uint64_t t = __shfl_sync(kFull, v[j], rk & 31);
+                    if (j == (rk >> 5)) kk = t;
+                }
+                const unsigned kb = static_cast<unsigned>(kk >> 32);
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    if (32 * j + lane < m) {
+                        const unsigned u = static_cast<unsigned>(v[j] >> 32);
+                        const int w = static_cast<int>(static_cast<int64_t>(v[j] & 0xffffffffull) / seg);
+                        if (u < kb) atomicAdd(&sh.warp_lt[w], 1);
+                        else if (u == kb) atomicAdd(&sh.warp_eq[w], 1);
+                    }
+                }
+                if (lane == 0) sh.kth = kb;
+            }
+            __syncthreads();
+            kth = sh.kth;
+        } else {
+        // bitonic sort of the bucket, padded to a power of two with ~0
         int len = 1;
         while (len < m) len <<= 1;
         for (int i = m + threadIdx.x; i < len; i += kSelThreads) sh.cand[i] = ~0ull;
@@ -319,6 +358,7 @@ row_select_kernel(float* __restrict__ tile, const float* __restrict__ norms, int
             else if (u == kth) atomicAdd(&sh.warp_eq[w], 1);
         }
         __syncthreads();
+        }
     }
 
     // first slot of each segment: exclusive scans over the warps' counts
