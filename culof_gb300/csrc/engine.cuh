@@ -173,6 +173,9 @@ private:
     // the FP32 sweep's evaluated (warp x column tile) blocks; the total it
     // would evaluate without pruning
     DevBuf pair_stats_, boxes_, plist_, pcount_, order_;
+    // isolated rows of the small-d sweep: threshold, count, list and flags;
+    // dimension-major columns and quarter-tile boxes
+    DevBuf iso_, iso_cols_;
     unsigned long long stat_total_blocks_ = 0;
     // Device status word of the current call: kernels set it (a bounded wait
     // that expired, an out-of-range neighbour index); host paths check it.

@@ -32,6 +32,8 @@
 // index), identical to the general path and the oracle; the filter only
 // decides which pairs get an exact evaluation, and its bound is proven
 // conservative (tau_from below).
+#include <cuda_bf16.h>
+
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
@@ -428,18 +430,51 @@ __global__ void order_key_kernel(const int* __restrict__ pcount, int t0, int mt,
 template <int DP>
 __global__ void __launch_bounds__(256) prune_list_kernel(const float* __restrict__ boxes, int nt, int t0, int qs,
                                                          const unsigned long long* __restrict__ kth_seed,
-                                                         uint2* __restrict__ plist, int* __restrict__ pcount) {
+                                                         uint2* __restrict__ plist, int* __restrict__ pcount,
+                                                         const float* __restrict__ tiles,
+                                                         const unsigned char* __restrict__ iso_flag) {
     __shared__ float tbox[2][DP];
+    __shared__ float wbox[4][2][DP];
     __shared__ float kmax_s;
     __shared__ int wtot[8];
     __shared__ int base_s;
     const int T = t0 + static_cast<int>(blockIdx.x);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (threadIdx.x < 2 * DP) tbox[threadIdx.x / DP][threadIdx.x % DP] = boxes[static_cast<int64_t>(T) * 2 * DP + threadIdx.x];
+    if (!iso_flag) {
+        if (threadIdx.x < 2 * DP)
+            tbox[threadIdx.x / DP][threadIdx.x % DP] = boxes[static_cast<int64_t>(T) * 2 * DP + threadIdx.x];
+    } else if (warp < 4) {
+        // the box of the rows that stay in the sweep (isolated rows take
+        // their own pass; a tile with none gets an empty box)
+        const float* own = tiles + static_cast<int64_t>(T) * tile_floats(DP);
+        const int r = threadIdx.x;
+        const bool keep = reinterpret_cast<const unsigned*>(own)[tile_index_off(DP) + r] != kNoIndex &&
+                          !iso_flag[static_cast<int64_t>(T) * kRT + r];
+#pragma unroll
+        for (int f = 0; f < DP; ++f) {
+            float lo = keep ? tile_coord<DP>(own, r, f) : __int_as_float(0x7f800000);
+            float hi = keep ? tile_coord<DP>(own, r, f) : __int_as_float(0xff800000);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+                hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+            }
+            if (lane == 0) {
+                wbox[warp][0][f] = lo;
+                wbox[warp][1][f] = hi;
+            }
+        }
+    }
     if (warp == 0) {
+        const unsigned* own_idx =
+            iso_flag ? reinterpret_cast<const unsigned*>(tiles + static_cast<int64_t>(T) * tile_floats(DP)) +
+                           tile_index_off(DP)
+                     : nullptr;
         float v = __int_as_float(0xff800000);
         for (int r = lane; r < kRT; r += 32) {
-            const unsigned long long kk = kth_seed[static_cast<int64_t>(T) * kRT + r];
+            const int64_t pos = static_cast<int64_t>(T) * kRT + r;
+            if (iso_flag && (iso_flag[pos] || own_idx[r] == kNoIndex)) continue;  // not in the sweep
+            const unsigned long long kk = kth_seed[pos];
             v = fmaxf(v, kk == kKeyMax ? __int_as_float(0x7f800000) : __uint_as_float(key_bits(kk)));
         }
 #pragma unroll
@@ -448,6 +483,12 @@ __global__ void __launch_bounds__(256) prune_list_kernel(const float* __restrict
             kmax_s = v;
             base_s = 0;
         }
+    }
+    __syncthreads();
+    if (iso_flag && threadIdx.x < DP) {
+        const int f = threadIdx.x;
+        tbox[0][f] = fminf(fminf(wbox[0][0][f], wbox[1][0][f]), fminf(wbox[2][0][f], wbox[3][0][f]));
+        tbox[1][f] = fmaxf(fmaxf(wbox[0][1][f], wbox[1][1][f]), fmaxf(wbox[2][1][f], wbox[3][1][f]));
     }
     __syncthreads();
     const float kmax = kmax_s;
@@ -638,6 +679,349 @@ __global__ void __launch_bounds__(kThreads) seed_kernel(const float* __restrict_
     }
 }
 
+// ---------------------------------------------------------------- isolated rows
+//
+// A row whose seed k-th distance is among the largest (an isolated point:
+// its neighbours are far away, so its warp of the sweep can prune almost no
+// column tile) holds its warp busy on nearly every tile while the CTA's
+// other warps skip most of them, and the CTA lasts as long as its busiest
+// warp. About 1% of the rows, those with the largest seed k-th keys, leave
+// the sweep (it treats them like padding rows) and take a pass of their
+// own (iso_rows_kernel). Their result is the row's split-0 list, so the
+// merge reads it like a sweep result. Which rows move is a performance
+// choice only: every row's k best are exact either way.
+constexpr int kIsoSamples = 1024;  // seed k-th keys sampled for the threshold (one per thread)
+constexpr int kIsoTop = 10;        // rows above the 11th largest sample leave (about 1%)
+constexpr int kIsoMaxTiles = 8192;  // the pass keeps 4 gaps of 2 bytes per column tile in shared memory
+
+// One block of kIsoSamples threads: the seed k-th keys of kIsoSamples rows
+// spread evenly over the valid positions [pos0, pos1); the threshold is the
+// (kIsoTop+1)-th largest (each thread counts the samples above its own).
+// Also zeroes the row counter.
+__global__ void __launch_bounds__(kIsoSamples) iso_threshold_kernel(const unsigned long long* __restrict__ kth_shared,
+                                                                     int64_t pos0, int64_t pos1,
+                                                                     unsigned long long* __restrict__ thr,
+                                                                     int* __restrict__ iso_count) {
+    __shared__ __align__(16) uint64_t smp[kIsoSamples];
+    const int i = threadIdx.x;
+    const int64_t len = pos1 - pos0;
+    const uint64_t mine = len > 0 ? kth_shared[pos0 + len * i / kIsoSamples] : kKeyMax;
+    smp[i] = mine;
+    __syncthreads();
+    int above = 0, same = 0;
+    const ulonglong2* smp2 = reinterpret_cast<const ulonglong2*>(smp);
+#pragma unroll 8
+    for (int j = 0; j < kIsoSamples / 2; ++j) {
+        const ulonglong2 o = smp2[j];
+        above += (o.x > mine ? 1 : 0) + (o.y > mine ? 1 : 0);
+        same += (o.x == mine ? 1 : 0) + (o.y == mine ? 1 : 0);
+    }
+    if (above <= kIsoTop && above + same > kIsoTop) *thr = mine;  // every such thread holds the same key
+    if (i == 0) *iso_count = 0;
+}
+
+// Positions [pos0, pend) of the row tiles: flag[pos] = 1 for the valid rows
+// (pos < n) whose seed k-th key exceeds the threshold, up to cap of them,
+// and their positions listed (in no particular order; *iso_count may pass
+// cap, the list holds min(*iso_count, cap)).
+__global__ void iso_mark_kernel(const unsigned long long* __restrict__ kth_shared, int64_t pos0, int64_t pend,
+                                int64_t n, const unsigned long long* __restrict__ thr, int cap,
+                                unsigned char* __restrict__ flag, int* __restrict__ iso_list,
+                                int* __restrict__ iso_count) {
+    const unsigned long long t = *thr;
+    const int lane = threadIdx.x & 31;
+    for (int64_t b = pos0 + static_cast<int64_t>(blockIdx.x) * blockDim.x; b < pend;
+         b += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const int64_t pos = b + threadIdx.x;
+        bool iso = pos < pend && pos < n && kth_shared[pos] > t;
+        const unsigned m = __ballot_sync(0xffffffffu, iso);
+        if (m) {
+            const int leader = __ffs(m) - 1;
+            int base = 0;
+            if (lane == leader) base = atomicAdd(iso_count, __popc(m));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            const int slot = base + __popc(m & ((1u << lane) - 1u));
+            iso = iso && slot < cap;
+            if (iso) iso_list[slot] = static_cast<int>(pos);
+        }
+        if (pos < pend) flag[pos] = iso ? 1 : 0;
+    }
+}
+
+// The k best keys below a bound, kept by one warp: for k <= 32 the 32 best
+// so far sorted across the warp (one per lane) with up to 32 pending keys in
+// shared memory; for k > 32 a sorted prefix of at most k keys plus up to 32
+// new ones in shared memory (buf holds 96 keys). bound only decreases: the
+// smaller of the caller's bound and the k-th key held.
+// Out of line (one copy of the sorting networks for every call site): merges
+// the pending keys of a WarpBest (see below) and tightens its bound.
+__device__ __noinline__ void warp_best_flush(uint64_t* buf, int k, uint64_t& bound, uint64_t& best, int& cnt,
+                                             int& sorted) {
+    const int lane = threadIdx.x & 31;
+    if (k <= 32) {
+        uint64_t w[1] = {lane < cnt ? buf[lane] : kKeyMax};
+        warp_bitonic_sort<1>(w);
+        best = warp_merge_lowest32(best, w[0]);
+        const uint64_t kth = __shfl_sync(0xffffffffu, best, k - 1);
+        bound = kth < bound ? kth : bound;
+        cnt = 0;
+    } else {
+        uint64_t sel;
+        cnt = merge_sorted_prefix<1>(buf, sorted, cnt, k, k - 1, [](uint64_t key) { return key; }, &sel);
+        sorted = cnt;
+        bound = sel < bound ? sel : bound;
+    }
+    __syncwarp();
+}
+
+struct WarpBest {
+    uint64_t* buf;
+    int k;
+    uint64_t bound;
+    uint64_t best = kKeyMax;
+    int cnt = 0;     // k <= 32: pending keys; k > 32: buffer length
+    int sorted = 0;  // k > 32: buf[0..sorted) is sorted
+
+    __device__ __forceinline__ void flush() { warp_best_flush(buf, k, bound, best, cnt, sorted); }
+    // every lane offers one key (kKeyMax: none)
+    __device__ __forceinline__ void offer(uint64_t key) {
+        const int lane = threadIdx.x & 31;
+        unsigned m = __ballot_sync(0xffffffffu, key < bound);
+        if (m && cnt + __popc(m) > (k <= 32 ? 32 : sorted + 32)) {
+            __syncwarp();
+            flush();
+            m = __ballot_sync(0xffffffffu, key < bound);
+        }
+        if (m) {
+            if (key < bound) buf[cnt + __popc(m & ((1u << lane) - 1u))] = key;
+            cnt += __popc(m);
+            __syncwarp();
+        }
+    }
+    __device__ __forceinline__ void finish() {
+        if (cnt > (k <= 32 ? 0 : sorted)) flush();
+    }
+    // after finish(): key e of the k best (sorted ascending, kKeyMax padded);
+    // for k <= 32 only lane e's own element (e == lane) is available
+    __device__ __forceinline__ uint64_t get(int e) const {
+        if (k <= 32) return best;
+        return e < sorted ? buf[e] : kKeyMax;
+    }
+};
+
+// Quarter tiles: the pass prunes 32-column quarters of a tile (tighter
+// boxes than whole tiles around isolated points) and reads a dimension-major
+// copy of the column coordinates, so one quarter is DP coalesced 128-byte
+// loads: cols[(t * DP + f) * kCT + c] = coordinate f of column c of tile t.
+constexpr int kQuarter = 32;
+constexpr int kQuarters = kCT / kQuarter;
+
+template <int DP>
+__global__ void iso_cols_kernel(const float* __restrict__ tiles, int nt, float* __restrict__ cols) {
+    const int64_t total = static_cast<int64_t>(nt) * DP * kCT;
+    for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < total;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const int64_t t = i / (DP * kCT);
+        const int f = static_cast<int>(i / kCT % DP), c = static_cast<int>(i % kCT);
+        cols[i] = tile_coord<DP>(tiles + t * tile_floats(DP), c, f);
+    }
+}
+
+// One warp per quarter: the bounding box of its valid columns as a 32-byte
+// record of 16 bf16 values, qbox[16 q + f] = lower bound of dimension f
+// rounded down, qbox[16 q + 8 + f] = upper bound rounded up (a box that
+// contains the float32 one; +inf / -inf when the quarter has no valid
+// column; unused slots 0), for quarter q = 4 t + j.
+template <int DP>
+__global__ void iso_qbox_kernel(const float* __restrict__ tiles, const float* __restrict__ cols, int nt,
+                                __nv_bfloat16* __restrict__ qbox) {
+    const int lane = threadIdx.x & 31;
+    const int64_t nq = static_cast<int64_t>(nt) * kQuarters;
+    for (int64_t q = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) / 32; q < nq;
+         q += static_cast<int64_t>(gridDim.x) * blockDim.x / 32) {
+        const int64_t t = q / kQuarters;
+        const int c = static_cast<int>(q % kQuarters) * kQuarter + lane;
+        const bool valid =
+            reinterpret_cast<const unsigned*>(tiles + t * tile_floats(DP))[tile_index_off(DP) + c] != kNoIndex;
+        float mine = 0.0f;  // lane f: lower bound of dimension f; lane 8 + f: upper bound
+#pragma unroll
+        for (int f = 0; f < DP; ++f) {
+            const float v = cols[(t * DP + f) * kCT + c];
+            float lo = valid ? v : __int_as_float(0x7f800000), hi = valid ? v : __int_as_float(0xff800000);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+                hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+            }
+            if (lane == f) mine = lo;
+            if (lane == 8 + f) mine = hi;
+        }
+        if (lane < 16)
+            qbox[16 * q + lane] = lane < 8 ? __float2bfloat16_rd(mine) : __float2bfloat16_ru(mine);
+    }
+}
+
+// Gaps are kept as the upper 16 bits of their float32 bit pattern
+// (non-negative floats truncated: rounded down, so pruning stays
+// conservative); kGapSkip marks a quarter the pass never visits.
+constexpr uint16_t kGapSkip = 0xFFFFu;
+__device__ __forceinline__ uint16_t gap_bits_down(float g) { return static_cast<uint16_t>(__float_as_uint(g) >> 16); }
+// the smallest 16-bit pattern not below distance b (+inf: 0x7F80)
+__device__ __forceinline__ unsigned bound_bits_up(float b) { return (__float_as_uint(b) + 0xFFFFu) >> 16; }
+
+// One warp: up to kIsoBatch quarters q[0..m) against point a (the seed's
+// exact arithmetic: dimensions in order), every key offered. Lane l takes
+// column l of each quarter; all loads are issued first.
+constexpr int kIsoBatch = 4;
+template <int DP>
+__device__ __forceinline__ void iso_eval_quarters(const float* __restrict__ tiles, const float* __restrict__ cols,
+                                                  const int (&q)[kIsoBatch], int m, const float (&a)[DP],
+                                                  WarpBest& wb) {
+    const int lane = threadIdx.x & 31;
+    float x[kIsoBatch][DP];
+    unsigned ix[kIsoBatch];
+#pragma unroll
+    for (int i = 0; i < kIsoBatch; ++i) {
+        const int qi = q[i < m ? i : 0];
+        const int64_t t = qi / kQuarters;
+        const int c = (qi % kQuarters) * kQuarter + lane;
+#pragma unroll
+        for (int f = 0; f < DP; ++f) x[i][f] = cols[(t * DP + f) * kCT + c];
+        ix[i] = reinterpret_cast<const unsigned*>(tiles + t * tile_floats(DP))[tile_index_off(DP) + c];
+    }
+#pragma unroll
+    for (int i = 0; i < kIsoBatch; ++i) {
+        if (i >= m) break;
+        float d2 = 0.0f;
+#pragma unroll
+        for (int f = 0; f < DP; ++f) {
+            const float t = __fsub_rn(a[f], x[i][f]);
+            d2 = __fmaf_rn(t, t, d2);
+        }
+        wb.offer(ix[i] != kNoIndex ? make_key(__float_as_uint(d2), ix[i]) : kKeyMax);
+    }
+}
+
+// One CTA (kIsoWarps warps) per listed row: its k best keys (sorted,
+// kKeyMax padded) over the column tiles outside the seed window of its row
+// tile, below its seed k-th key, written to out[pos * k ..].
+//  1. The rounded-down gap between the point and every quarter's box
+//     (coalesced, into shared memory; the window's quarters are skipped).
+//  2. Warp w owns quarter w of every tile (the quarters near the point are
+//     spread over all warps) and visits its quarters in three rounds of
+//     growing gap: gaps up to 1/16 of the row's current bound, then 1/4,
+//     then the whole bound, so that the bound tightens on the nearest
+//     quarters before the far ones are tested; quarters within the bound
+//     are evaluated kIsoBatch at a time.
+//  3. The warps share the bound (the smallest of the seed's k-th key and
+//     their own k-th keys) in shared memory and merge their lists at the
+//     end.
+constexpr int kIsoWarps = 4;
+template <int DP>
+__global__ void __launch_bounds__(32 * kIsoWarps, 6) iso_rows_kernel(const float* __restrict__ tiles,
+                                                                    const float* __restrict__ cols,
+                                                                    const __nv_bfloat16* __restrict__ qbox, int nt, int qs,
+                                                                    int k, int cap, const int* __restrict__ iso_list,
+                                                                    const int* __restrict__ iso_count,
+                                                                    const unsigned long long* __restrict__ kth_shared,
+                                                                    uint64_t* __restrict__ out) {
+    extern __shared__ __align__(16) uint16_t qgap_s[];  // 4 per tile
+    __shared__ uint64_t wl[kIsoWarps][96];              // per warp: WarpBest's buffer
+    __shared__ uint64_t fin[kIsoWarps][kMaxK];         // per warp: its k best at the end
+    __shared__ unsigned long long bound_s;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int count = min(*iso_count, cap);
+    const int nb = (nt + 31) / 32;
+    const int64_t nq = static_cast<int64_t>(nt) * kQuarters;
+    // the seed window: spiral positions 0..qs-1, offsets -(qs-1)/2 .. qs/2
+    const int wlo = (qs - 1) / 2, whi = qs / 2;
+    for (int h = blockIdx.x; h < count; h += gridDim.x) {
+        const int64_t pos = iso_list[h];
+        const int T = static_cast<int>(pos / kRT), r = static_cast<int>(pos % kRT);
+        const float* own = tiles + static_cast<int64_t>(T) * tile_floats(DP);
+        float a[DP];
+#pragma unroll
+        for (int f = 0; f < DP; ++f) a[f] = tile_coord<DP>(own, r, f);
+        if (threadIdx.x == 0) bound_s = kth_shared[pos];
+#pragma unroll 4
+        for (int q = threadIdx.x; q < nq; q += 32 * kIsoWarps) {
+            const int t = q / kQuarters;
+            int off = t - T;  // offset from the row tile, in (-nt/2, nt/2]
+            if (off > nt / 2) off -= nt;
+            if (off <= -((nt + 1) / 2)) off += nt;
+            const uint4 lo4 = reinterpret_cast<const uint4*>(qbox)[2 * q];
+            const uint4 hi4 = reinterpret_cast<const uint4*>(qbox)[2 * q + 1];
+            const unsigned lw[4] = {lo4.x, lo4.y, lo4.z, lo4.w}, hw[4] = {hi4.x, hi4.y, hi4.z, hi4.w};
+            float g2 = 0.0f;
+#pragma unroll
+            for (int f = 0; f < DP; ++f) {  // bf16 to float is exact: the bits shifted up
+                const float lo = __uint_as_float((f & 1 ? lw[f >> 1] >> 16 : lw[f >> 1] & 0xFFFFu) << 16);
+                const float hi = __uint_as_float((f & 1 ? hw[f >> 1] >> 16 : hw[f >> 1] & 0xFFFFu) << 16);
+                const float gap = fmaxf(0.0f, fmaxf(__fsub_rd(lo, a[f]), __fsub_rd(a[f], hi)));
+                g2 = __fadd_rd(g2, __fmul_rd(gap, gap));
+            }
+            qgap_s[q] = (off >= -wlo && off <= whi) ? kGapSkip : gap_bits_down(__fmul_rd(g2, kPruneShrink));
+        }
+        __syncthreads();
+        WarpBest wb{wl[warp], k, bound_s};
+        const auto shared_bound = [&]() {  // publish this warp's bound, take the CTA's
+            uint64_t sb = 0;
+            if (lane == 0) sb = atomicMin(&bound_s, static_cast<unsigned long long>(wb.bound));
+            sb = __shfl_sync(0xffffffffu, sb, 0);
+            if (sb < wb.bound) wb.bound = sb;
+        };
+        const auto bound_up = [&]() {
+            return wb.bound == kKeyMax ? 0xFFFEu : bound_bits_up(__uint_as_float(key_bits(wb.bound)));
+        };
+        int batch[kIsoBatch];  // quarters waiting for evaluation (warp-uniform)
+        int nbatch = 0;
+        unsigned lo_bits = 0;  // this round takes tiles whose gap lies in [lo_bits, hi_bits]
+        for (int round = 0; round < 3; ++round) {
+            shared_bound();
+            const float bd = wb.bound == kKeyMax ? __int_as_float(0x7f800000) : __uint_as_float(key_bits(wb.bound));
+            const float frac = round == 0 ? 0.0625f : round == 1 ? 0.25f : 1.0f;
+            unsigned hi_bits = bound_bits_up(bd * frac);
+            if (round == 2 || hi_bits > 0xFFFEu) hi_bits = 0xFFFEu;  // the last round takes every quarter left
+            if (hi_bits < lo_bits) continue;
+            for (int b = 0; b < nb; ++b) {
+                const int t = 32 * b + lane;
+                const unsigned g = t < nt ? qgap_s[kQuarters * t + warp] : kGapSkip;
+                unsigned todo = __ballot_sync(0xffffffffu, g >= lo_bits && g <= hi_bits && g <= bound_up());
+                while (todo) {
+                    const int src = __ffs(todo) - 1;
+                    todo &= todo - 1;
+                    if (__shfl_sync(0xffffffffu, g, src) > bound_up()) continue;  // a tighter bound prunes it
+                    batch[nbatch++] = (32 * b + src) * kQuarters + warp;
+                    if (nbatch == kIsoBatch) {
+                        iso_eval_quarters<DP>(tiles, cols, batch, nbatch, a, wb);
+                        nbatch = 0;
+                        shared_bound();
+                    }
+                }
+            }
+            lo_bits = hi_bits + 1;
+        }
+        if (nbatch > 0) iso_eval_quarters<DP>(tiles, cols, batch, nbatch, a, wb);
+        wb.finish();
+        for (int e = lane; e < k; e += 32) fin[warp][e] = wb.get(e);
+        __syncthreads();
+        // warp 0 merges the other warps' lists into its own, under the seed's
+        // k-th key (the shared bound may equal a key of those lists)
+        if (warp == 0) {
+            wb.bound = kth_shared[pos];
+            for (int w = 1; w < kIsoWarps; ++w)
+                for (int e0 = 0; e0 < k; e0 += 32) {
+                    const int e = e0 + lane;
+                    wb.offer(e < k ? fin[w][e] : kKeyMax);
+                }
+            wb.finish();
+            uint64_t* dst = out + pos * k;
+            for (int e = lane; e < k; e += 32) dst[e] = wb.get(e);
+        }
+        __syncthreads();
+    }
+}
+
 // ---------------------------------------------------------------- sweep
 
 template <int DP, int M>
@@ -701,7 +1085,8 @@ sweep_kernel(const float* __restrict__ tiles, int nt, int t0, int mt, int qs, in
              const unsigned* __restrict__ max_norm_bits,
              unsigned long long* __restrict__ kth_shared, uint64_t* __restrict__ partial, int* __restrict__ status,
              unsigned long long* __restrict__ evaluated_blocks, const uint2* __restrict__ plist,
-             const int* __restrict__ pcount, const unsigned* __restrict__ order, const float* __restrict__ boxes) {
+             const int* __restrict__ pcount, const unsigned* __restrict__ order, const float* __restrict__ boxes,
+             const unsigned char* __restrict__ iso_flag) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     SweepSmem<DP, M>& sh = *reinterpret_cast<SweepSmem<DP, M>*>(smem_raw);
     // row tiles with the longest candidate lists first (tail balance)
@@ -730,7 +1115,9 @@ sweep_kernel(const float* __restrict__ tiles, int nt, int t0, int mt, int qs, in
         const uint64_t kk = kth_shared[pos];
         sh.L.kth[tid] = kk;
         sh.L.row_norm[tid] = nr;
-        sh.L.tau[tid] = (reinterpret_cast<const unsigned*>(own)[tile_index_off(DP) + tid] == kNoIndex)
+        // padding rows and isolated rows (their own pass) take no candidates
+        sh.L.tau[tid] = (reinterpret_cast<const unsigned*>(own)[tile_index_off(DP) + tid] == kNoIndex ||
+                         (iso_flag && iso_flag[pos]))
                           ? __int_as_float(0xff800000)
                           : tau_from(kk, nr, nmax, DP);
         sh.L.cnt[tid] = 0;
@@ -774,7 +1161,8 @@ sweep_kernel(const float* __restrict__ tiles, int nt, int t0, int mt, int qs, in
     // (invalid rows take no candidates and do not count)
     const unsigned* own_idx = reinterpret_cast<const unsigned*>(own) + tile_index_off(DP);
     const int wrow = warp * kRowsPerWarp + (lane & 15);
-    const bool wvalid = own_idx[wrow] != kNoIndex;
+    const bool wvalid =
+        own_idx[wrow] != kNoIndex && !(iso_flag && iso_flag[static_cast<int64_t>(T) * kRT + wrow]);
 #pragma unroll
     for (int f = 0; f < DP; ++f) {
         float lo = wvalid ? sh.rowc[wrow][f] : __int_as_float(0x7f800000);
@@ -1079,6 +1467,17 @@ int grid_for(int64_t items, int block) {
     return static_cast<int>(g < 1 ? 1 : g);
 }
 
+// Whether isolated rows leave the small-d sweep (see iso_rows_kernel):
+// from kIsoMinPoints points on (clusters with 1% outliers, d = 8, k = 20:
+// 7.86 ms against 8.40 ms at 200,000 points, even at 100,000, 3% slower at
+// 50,000); CULOF_ISO_ROWS=0 or 1 forces the choice (the results are the
+// same either way).
+constexpr int64_t kIsoMinPoints = 100000;
+bool iso_rows_enabled(int64_t n) {
+    if (const char* env = std::getenv("CULOF_ISO_ROWS")) return env[0] != '0';
+    return n >= kIsoMinPoints;
+}
+
 }  // namespace
 
 int choose_splits(int nt, int sms) {
@@ -1096,11 +1495,12 @@ template <int DP, int M>
 void launch_sweep(const float* tiles, int nt, int t0, int mt, int qs, int nsplit, int k, const unsigned* maxn,
                   unsigned long long* kth_shared,
                   uint64_t* partial, int* status, unsigned long long* evaluated, const uint2* plist, const int* pcount,
-                  const unsigned* order, const float* boxes, cudaStream_t s) {
+                  const unsigned* order, const float* boxes, const unsigned char* iso_flag, cudaStream_t s) {
     const size_t smem = sizeof(SweepSmem<DP, M>);
     set_max_dynamic_smem(reinterpret_cast<const void*>(sweep_kernel<DP, M>), static_cast<int>(smem));
     sweep_kernel<DP, M><<<mt * nsplit, kThreads, smem, s>>>(tiles, nt, t0, mt, qs, nsplit, k, maxn, kth_shared,
-                                                            partial, status, evaluated, plist, pcount, order, boxes);
+                                                            partial, status, evaluated, plist, pcount, order, boxes,
+                                                            iso_flag);
     CG_LAUNCH_CHECK();
 }
 
@@ -1296,6 +1696,28 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
     if (small) CG_LAUNCH_CHECK();
     mark(3);
 
+    // 3a. isolated rows (the FP32 small-d sweep): about 1% of the rows, those
+    // with the largest seed k-th keys, leave the sweep for their own pass
+    unsigned char* iso_flag = nullptr;
+    int* iso_list = nullptr;
+    int* iso_count = nullptr;
+    const int64_t pend = static_cast<int64_t>(t0 + mt) * kCT;
+    // at most about 2% of the rows (a sample threshold that ties with many
+    // equal k-th keys could otherwise take far more than 1%)
+    const int iso_cap = static_cast<int>((pos1 - pos0) / 50 + 32);
+    if (small && !tensor && sweep && mt > 0 && pos1 > pos0 && nt <= kIsoMaxTiles && iso_rows_enabled(n)) {
+        char* b = static_cast<char*>(iso_.get(256 + sizeof(int) * static_cast<size_t>(pend - pos0) + padded));
+        unsigned long long* thr = reinterpret_cast<unsigned long long*>(b);
+        iso_count = reinterpret_cast<int*>(b + sizeof(unsigned long long));
+        iso_list = reinterpret_cast<int*>(b + 256);
+        iso_flag = reinterpret_cast<unsigned char*>(iso_list + (pend - pos0));  // indexed by position
+        iso_threshold_kernel<<<1, kIsoSamples, 0, s>>>(kth_shared, pos0, pos1, thr, iso_count);
+        CG_LAUNCH_CHECK();
+        iso_mark_kernel<<<grid_for(pend - pos0, 256), 256, 0, s>>>(kth_shared, pos0, pend, n, thr, iso_cap, iso_flag,
+                                                                   iso_list, iso_count);
+        CG_LAUNCH_CHECK();
+    }
+
     // 3b. per row tile: the column tiles the seed's k-th distances leave
     uint2* plist = nullptr;
     int* pcount = nullptr;
@@ -1309,10 +1731,10 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
         plist = plist_.as<uint2>(static_cast<size_t>(nt) * nt);
         pcount = pcount_.as<int>(nt);
         switch (dp) {
-            case 2: prune_list_kernel<2><<<mt, 256, 0, s>>>(boxes, nt, t0, qs, kth_shared, plist, pcount); break;
-            case 4: prune_list_kernel<4><<<mt, 256, 0, s>>>(boxes, nt, t0, qs, kth_shared, plist, pcount); break;
-            case 6: prune_list_kernel<6><<<mt, 256, 0, s>>>(boxes, nt, t0, qs, kth_shared, plist, pcount); break;
-            default: prune_list_kernel<8><<<mt, 256, 0, s>>>(boxes, nt, t0, qs, kth_shared, plist, pcount); break;
+            case 2: prune_list_kernel<2><<<mt, 256, 0, s>>>(boxes, nt, t0, qs, kth_shared, plist, pcount, tiles, iso_flag); break;
+            case 4: prune_list_kernel<4><<<mt, 256, 0, s>>>(boxes, nt, t0, qs, kth_shared, plist, pcount, tiles, iso_flag); break;
+            case 6: prune_list_kernel<6><<<mt, 256, 0, s>>>(boxes, nt, t0, qs, kth_shared, plist, pcount, tiles, iso_flag); break;
+            default: prune_list_kernel<8><<<mt, 256, 0, s>>>(boxes, nt, t0, qs, kth_shared, plist, pcount, tiles, iso_flag); break;
         }
         CG_LAUNCH_CHECK();
     }
@@ -1346,9 +1768,9 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
         const bool big = k > 24;
 #define CG_SWEEP(DPV)                                                                                              \
     (big ? launch_sweep<DPV, 96>(tiles, nt, t0, mt, qs, nsplit, k, maxn, kth_shared, partial, status, evaluated, plist, \
-                                 pcount, order, boxes, s)                                                           \
+                                 pcount, order, boxes, iso_flag, s)                                                 \
          : launch_sweep<DPV, 64>(tiles, nt, t0, mt, qs, nsplit, k, maxn, kth_shared, partial, status, evaluated, plist, \
-                                 pcount, order, boxes, s))
+                                 pcount, order, boxes, iso_flag, s))
         switch (dp) {
             case 2: CG_SWEEP(2); break;
             case 4: CG_SWEEP(4); break;
@@ -1356,6 +1778,30 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
             default: CG_SWEEP(8); break;
         }
 #undef CG_SWEEP
+    }
+    if (iso_flag) {  // the isolated rows' own pass: their split-0 lists
+        const int g = 6 * sms;  // one CTA per row, grid-stride (six CTAs per SM)
+        const size_t qgap_bytes = sizeof(uint16_t) * kQuarters * static_cast<size_t>(nt);
+        // columns (nt x kCT x dp floats), then the quarter boxes (32 bytes each)
+        float* cols = iso_cols_.as<float>(static_cast<size_t>(nt) * (kCT * dp + kQuarters * 8));
+        __nv_bfloat16* qbox = reinterpret_cast<__nv_bfloat16*>(cols + static_cast<size_t>(nt) * kCT * dp);
+        constexpr size_t kDefaultDynamicSmem = 40 * 1024;
+#define CG_ISO(DPV)                                                                                                \
+    iso_cols_kernel<DPV><<<grid_for(static_cast<int64_t>(nt) * DPV * kCT, 256), 256, 0, s>>>(tiles, nt, cols);   \
+    iso_qbox_kernel<DPV><<<grid_for(static_cast<int64_t>(nt) * kQuarters * 32, 256), 256, 0, s>>>(tiles, cols, nt, \
+                                                                                                   qbox);          \
+    if (qgap_bytes > kDefaultDynamicSmem)                                                                          \
+        set_max_dynamic_smem(reinterpret_cast<const void*>(iso_rows_kernel<DPV>), static_cast<int>(qgap_bytes));  \
+    iso_rows_kernel<DPV><<<g, 32 * kIsoWarps, qgap_bytes, s>>>(tiles, cols, qbox, nt, qs, k, iso_cap, iso_list,    \
+                                                               iso_count, kth_shared, partial)
+        switch (dp) {
+            case 2: CG_ISO(2); break;
+            case 4: CG_ISO(4); break;
+            case 6: CG_ISO(6); break;
+            default: CG_ISO(8); break;
+        }
+#undef CG_ISO
+        CG_LAUNCH_CHECK();
     }
     const int ns = sweep ? nsplit : 0;
     mark(4);

@@ -124,6 +124,40 @@ def test_knn_without_prune_lists_bit_exact(ctx, monkeypatch, name):
     np.testing.assert_array_equal(d2.view(np.uint32), o_d2.view(np.uint32))
 
 
+ISO_CASES = ["clusters", "clusters_k1", "lowdim", "d5_k25", "ragged", "dups", "k64", "k33_d3", "k32", "d1",
+             "dups_heavy"]
+
+
+@pytest.mark.parametrize("lists", ["1", "0"])
+@pytest.mark.parametrize("name", ISO_CASES)
+def test_knn_with_isolated_rows_bit_exact(ctx, monkeypatch, name, lists):
+    # the rows with the largest seed k-th keys (about 1%) leave the small-d
+    # sweep for their own pass from 65,536 points on; CULOF_ISO_ROWS=1 takes
+    # that path at any size, with and without the per-tile candidate lists
+    monkeypatch.setenv("CULOF_ISO_ROWS", "1")
+    monkeypatch.setenv("CULOF_PRUNE_LISTS", lists)
+    make, k = {c[0]: (c[1], c[2]) for c in KNN_CASES}[name]
+    X = make()
+    ctx.set_path(_culof.PATH_FAST)
+    idx, d2, kd = run_knn(ctx, X, k)
+    Xc, _, _ = oracle.center(X)
+    o_idx, o_d2, o_kd = oracle.knn(Xc, k)
+    np.testing.assert_array_equal(kd.view(np.uint32), o_kd.view(np.uint32))
+    np.testing.assert_array_equal(idx, o_idx)
+    np.testing.assert_array_equal(d2.view(np.uint32), o_d2.view(np.uint32))
+
+
+@pytest.mark.parametrize("iso", ["0", "1"])
+@pytest.mark.parametrize("k", [20, 40])
+def test_isolated_rows_do_not_change_lof(ctx, monkeypatch, iso, k):
+    # 30,000 points: 235 row tiles and isolated rows in most of them
+    monkeypatch.setenv("CULOF_ISO_ROWS", iso)
+    X = synthetic.clusters_with_outliers(30_000, 8, seed=41)
+    ctx.set_path(_culof.PATH_FAST)
+    got = ctx.lof(X, k)
+    np.testing.assert_array_equal(got.view(np.uint32), oracle.lof(X, k).view(np.uint32))
+
+
 def test_auto_selects_the_fast_path_for_small_d(ctx):
     X = synthetic.clusters_with_outliers(6000, 8, seed=1)
     ctx.lof(X, 20)
