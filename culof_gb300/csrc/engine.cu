@@ -108,11 +108,33 @@ Engine::~Engine() {
     if (bgraph_exec_) cudaGraphExecDestroy(bgraph_exec_);
     for (auto& e : events_)
         if (e) cudaEventDestroy(e);
+    for (cudaStream_t st : {high_stream_, side_stream_})
+        if (st) {
+            cudaSetDevice(device_);
+            cudaStreamSynchronize(st);
+            cudaStreamDestroy(st);
+        }
+    for (cudaEvent_t e : {fork_ev_, high_join_, side_join_})
+        if (e) cudaEventDestroy(e);
     if (own_stream_) {
         cudaSetDevice(device_);
         cudaStreamSynchronize(own_stream_);
         cudaStreamDestroy(own_stream_);
     }
+}
+
+void Engine::make_fork_streams() {
+    if (side_stream_) return;
+    // non-blocking (they must not wait for the legacy default stream); the
+    // high one of the greatest priority, the side one of the least, so that
+    // of two kernels that become ready together the high one's CTAs are
+    // dispatched first
+    int least = 0, greatest = 0;
+    CG_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    CG_CUDA(cudaStreamCreateWithPriority(&high_stream_, cudaStreamNonBlocking, greatest));
+    CG_CUDA(cudaStreamCreateWithPriority(&side_stream_, cudaStreamNonBlocking, least));
+    for (cudaEvent_t* e : {&fork_ev_, &high_join_, &side_join_})
+        CG_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
 }
 
 // pipeline.cu:99-110: CULOF_TILE_ROWS overrides; otherwise a 2 GiB cap on

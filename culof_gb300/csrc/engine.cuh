@@ -145,6 +145,13 @@ private:
     int device_;
     cudaStream_t own_stream_ = nullptr;
     cudaStream_t stream_ = nullptr;
+    // Two streams forked from the call's stream for work that runs side by
+    // side (the small-d sweep on the high one, the isolated rows' pass on
+    // the side one), with the events that fork them and join them back;
+    // created on first use.
+    cudaStream_t high_stream_ = nullptr, side_stream_ = nullptr;
+    cudaEvent_t fork_ev_ = nullptr, high_join_ = nullptr, side_join_ = nullptr;
+    void make_fork_streams();
     int path_ = kPathAuto;
     int last_path_ = kPathAuto;
 

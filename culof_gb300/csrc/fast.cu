@@ -690,8 +690,8 @@ __global__ void __launch_bounds__(kThreads) seed_kernel(const float* __restrict_
 // own (iso_rows_kernel). Their result is the row's split-0 list, so the
 // merge reads it like a sweep result. Which rows move is a performance
 // choice only: every row's k best are exact either way.
-constexpr int kIsoSamples = 1024;  // seed k-th keys sampled for the threshold (one per thread)
-constexpr int kIsoTop = 10;        // rows above the 11th largest sample leave (about 1%)
+constexpr int kIsoSamples = 512;  // seed k-th keys sampled for the threshold (one per thread)
+constexpr int kIsoTop = 5;        // rows above the 6th largest sample leave (about 1%)
 constexpr int kIsoMaxTiles = 8192;  // the pass keeps 4 gaps of 2 bytes per column tile in shared memory
 
 // One block of kIsoSamples threads: the seed k-th keys of kIsoSamples rows
@@ -1379,9 +1379,11 @@ sweep_kernel(const float* __restrict__ tiles, int nt, int t0, int mt, int qs, in
         __syncthreads();
         return;
     }
-    // final: this split's sorted k best per row; share the k-th key
+    // final: this split's sorted k best per row; share the k-th key (an
+    // isolated row's split-0 list is written by its own pass)
     for (int i = 0; i < kRowsPerWarp; ++i) {
         const int r = warp * kRowsPerWarp + i;
+        if (split == 0 && iso_flag && iso_flag[static_cast<int64_t>(T) * kRT + r]) continue;
         compact_row<M>(sh.L, r, k, nmax, DP);
         const int64_t pos = static_cast<int64_t>(T) * kRT + r;
         const int c = sh.L.cnt[r];
@@ -1468,11 +1470,11 @@ int grid_for(int64_t items, int block) {
 }
 
 // Whether isolated rows leave the small-d sweep (see iso_rows_kernel):
-// from kIsoMinPoints points on (clusters with 1% outliers, d = 8, k = 20:
-// 7.86 ms against 8.40 ms at 200,000 points, even at 100,000, 3% slower at
-// 50,000); CULOF_ISO_ROWS=0 or 1 forces the choice (the results are the
-// same either way).
-constexpr int64_t kIsoMinPoints = 100000;
+// from kIsoMinPoints points on (clusters with 1% outliers, d = 8, k = 20,
+// fit_predict: 7.72 ms against 8.39 ms at 200,000 points, 3.07 against
+// 3.15 at 100,000, 0.82 against 0.92 at 20,000); CULOF_ISO_ROWS=0 or 1
+// forces the choice (the results are the same either way).
+constexpr int64_t kIsoMinPoints = 16384;
 bool iso_rows_enabled(int64_t n) {
     if (const char* env = std::getenv("CULOF_ISO_ROWS")) return env[0] != '0';
     return n >= kIsoMinPoints;
@@ -1753,6 +1755,16 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
     // 4. sweep over the other tiles, split S ways
     unsigned long long* evaluated = reinterpret_cast<unsigned long long*>(pair_stats_.get(2 * sizeof(unsigned long long)));
     CG_CUDA(cudaMemsetAsync(evaluated, 0, 2 * sizeof(unsigned long long), s));
+    // With isolated rows, the sweep and their pass become ready together on
+    // two forked streams, the sweep's of higher priority: its CTAs are
+    // dispatched first and the pass fills the SMs its last wave leaves.
+    cudaStream_t sweep_s = s;
+    if (iso_flag) {
+        make_fork_streams();
+        CG_CUDA(cudaEventRecord(fork_ev_, s));
+        CG_CUDA(cudaStreamWaitEvent(high_stream_, fork_ev_, 0));
+        sweep_s = high_stream_;
+    }
     // every (warp, column tile) block past the seed window
     stat_total_blocks_ = (small && !tensor && sweep) ? static_cast<unsigned long long>(mt) * (nt - qs) * kWarps : 0;
     if (sweep && mt > 0 && tensor) {
@@ -1768,9 +1780,9 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
         const bool big = k > 24;
 #define CG_SWEEP(DPV)                                                                                              \
     (big ? launch_sweep<DPV, 96>(tiles, nt, t0, mt, qs, nsplit, k, maxn, kth_shared, partial, status, evaluated, plist, \
-                                 pcount, order, boxes, iso_flag, s)                                                 \
+                                 pcount, order, boxes, iso_flag, sweep_s)                                           \
          : launch_sweep<DPV, 64>(tiles, nt, t0, mt, qs, nsplit, k, maxn, kth_shared, partial, status, evaluated, plist, \
-                                 pcount, order, boxes, iso_flag, s))
+                                 pcount, order, boxes, iso_flag, sweep_s))
         switch (dp) {
             case 2: CG_SWEEP(2); break;
             case 4: CG_SWEEP(4); break;
@@ -1779,7 +1791,11 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
         }
 #undef CG_SWEEP
     }
-    if (iso_flag) {  // the isolated rows' own pass: their split-0 lists
+    if (iso_flag) {  // the isolated rows' own pass (split-0 lists), on the side stream
+        CG_CUDA(cudaEventRecord(high_join_, high_stream_));
+        CG_CUDA(cudaStreamWaitEvent(s, high_join_, 0));
+        cudaStream_t side = side_stream_;
+        CG_CUDA(cudaStreamWaitEvent(side, fork_ev_, 0));
         const int g = 6 * sms;  // one CTA per row, grid-stride (six CTAs per SM)
         const size_t qgap_bytes = sizeof(uint16_t) * kQuarters * static_cast<size_t>(nt);
         // columns (nt x kCT x dp floats), then the quarter boxes (32 bytes each)
@@ -1787,12 +1803,12 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
         __nv_bfloat16* qbox = reinterpret_cast<__nv_bfloat16*>(cols + static_cast<size_t>(nt) * kCT * dp);
         constexpr size_t kDefaultDynamicSmem = 40 * 1024;
 #define CG_ISO(DPV)                                                                                                \
-    iso_cols_kernel<DPV><<<grid_for(static_cast<int64_t>(nt) * DPV * kCT, 256), 256, 0, s>>>(tiles, nt, cols);   \
-    iso_qbox_kernel<DPV><<<grid_for(static_cast<int64_t>(nt) * kQuarters * 32, 256), 256, 0, s>>>(tiles, cols, nt, \
+    iso_cols_kernel<DPV><<<grid_for(static_cast<int64_t>(nt) * DPV * kCT, 256), 256, 0, side>>>(tiles, nt, cols);   \
+    iso_qbox_kernel<DPV><<<grid_for(static_cast<int64_t>(nt) * kQuarters * 32, 256), 256, 0, side>>>(tiles, cols, nt, \
                                                                                                    qbox);          \
     if (qgap_bytes > kDefaultDynamicSmem)                                                                          \
         set_max_dynamic_smem(reinterpret_cast<const void*>(iso_rows_kernel<DPV>), static_cast<int>(qgap_bytes));  \
-    iso_rows_kernel<DPV><<<g, 32 * kIsoWarps, qgap_bytes, s>>>(tiles, cols, qbox, nt, qs, k, iso_cap, iso_list,    \
+    iso_rows_kernel<DPV><<<g, 32 * kIsoWarps, qgap_bytes, side>>>(tiles, cols, qbox, nt, qs, k, iso_cap, iso_list,    \
                                                                iso_count, kth_shared, partial)
         switch (dp) {
             case 2: CG_ISO(2); break;
@@ -1802,6 +1818,8 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
         }
 #undef CG_ISO
         CG_LAUNCH_CHECK();
+        CG_CUDA(cudaEventRecord(side_join_, side));
+        CG_CUDA(cudaStreamWaitEvent(s, side_join_, 0));
     }
     const int ns = sweep ? nsplit : 0;
     mark(4);
