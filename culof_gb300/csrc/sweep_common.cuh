@@ -132,6 +132,28 @@ struct RowLists {
 // smallest; tighten the row's k-th key (only downwards) and its threshold.
 template <int M>
 __device__ void compact_row(RowLists<M>& L, int r, int k, float nmax, int dp) {
+    if constexpr (M <= 64) {
+        // nothing added since the last compaction: the list is already its
+        // sorted k best; at most 32 added: sort those and merge them with
+        // the sorted prefix (keys are unique: every pair is offered once)
+        const int c = min(L.cnt[r], M), s = L.sorted[r];
+        if (s >= 0 && s == c) return;
+        if (s >= 0 && s < c && c - s <= 32) {
+            uint64_t kk;
+            const int kept =
+                merge_sorted_prefix<1>(L.list[r], s, c, k, k - 1, [](uint64_t) { return kKeyMax; }, &kk);
+            if ((threadIdx.x & 31) == 0) {
+                L.cnt[r] = kept;
+                L.sorted[r] = kept;
+                if (kk != kKeyMax && kk < L.kth[r]) {
+                    L.kth[r] = kk;
+                    L.tau[r] = tau_from(kk, L.row_norm[r], nmax, dp);
+                }
+            }
+            __syncwarp();
+            return;
+        }
+    }
     if constexpr (M > 64) {
         // fast form for lists the full network sorts as 128 keys: sort only
         // the entries added since the last compaction (at most 64) and merge
