@@ -1804,8 +1804,10 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
         constexpr size_t kDefaultDynamicSmem = 40 * 1024;
 #define CG_ISO(DPV)                                                                                                \
     iso_cols_kernel<DPV><<<grid_for(static_cast<int64_t>(nt) * DPV * kCT, 256), 256, 0, side>>>(tiles, nt, cols);   \
+    CG_LAUNCH_CHECK();                                                                                             \
     iso_qbox_kernel<DPV><<<grid_for(static_cast<int64_t>(nt) * kQuarters * 32, 256), 256, 0, side>>>(tiles, cols, nt, \
                                                                                                    qbox);          \
+    CG_LAUNCH_CHECK();                                                                                             \
     if (qgap_bytes > kDefaultDynamicSmem)                                                                          \
         set_max_dynamic_smem(reinterpret_cast<const void*>(iso_rows_kernel<DPV>), static_cast<int>(qgap_bytes));  \
     iso_rows_kernel<DPV><<<g, 32 * kIsoWarps, qgap_bytes, side>>>(tiles, cols, qbox, nt, qs, k, iso_cap, iso_list,    \
