@@ -335,17 +335,20 @@ __global__ void build_tiles_kernel(const float* __restrict__ xc, const float* __
 
 // ---------------------------------------------------------------- seed
 
-// Exact distance (the oracle's formula) between column ca of tile ta and
-// column cb of tile tb.
+// Exact distances (the oracle's formula: t = a - b, s = fma(t, t, s) over the
+// dimensions in order) from row a (each coordinate duplicated into both
+// halves) to the two columns of pair p of a tile, with packed f32x2
+// instructions: per element the same IEEE operations as the scalar chain.
 template <int DP>
-__device__ __forceinline__ float tile_dist2(const float* ta, int ca, const float* tb, int cb) {
-    float s = 0.0f;
+__device__ __forceinline__ void pair_dist2(const float* tile, int p, const uint64_t (&a2)[DP], float& d0, float& d1) {
+    uint64_t s = 0;  // (+0, +0)
 #pragma unroll
     for (int f = 0; f < DP; ++f) {
-        const float t = __fsub_rn(tile_coord<DP>(ta, ca, f), tile_coord<DP>(tb, cb, f));
-        s = __fmaf_rn(t, t, s);
+        const uint64_t t = sub2(a2[f], *reinterpret_cast<const uint64_t*>(tile + p * pair_stride(DP) + 2 * f));
+        s = fma2(t, t, s);
     }
-    return s;
+    d0 = lo_f(s);
+    d1 = hi_f(s);
 }
 
 // Per row of tile T: the exact k best keys over the seed window (sorted,
@@ -544,15 +547,21 @@ __global__ void __launch_bounds__(kThreads) seed_kernel(const float* __restrict_
     for (int r = warp; r < kRT; r += kWarps) {
         const int64_t pos = static_cast<int64_t>(T) * kRT + r;
         const bool row_valid = idx[r] != kNoIndex;
-        // own tile: its 128 keys (the k best of them sorted below)
+        uint64_t ra2[DP];  // the row's coordinates, duplicated for the packed chains
+#pragma unroll
+        for (int f = 0; f < DP; ++f) ra2[f] = dup2(tile_coord<DP>(tile[0], r, f));
+        // own tile: its 128 keys (the k best of them sorted below); lane l
+        // takes the columns of pairs l and l + 32
         uint64_t v[4];
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const int c = j * 32 + lane;
-            uint64_t key = kKeyMax;
-            if (row_valid && c != r && idx[c] != kNoIndex)
-                key = make_key(__float_as_uint(tile_dist2<DP>(tile[0], r, tile[0], c)), idx[c]);
-            v[j] = key;
+        for (int h = 0; h < 2; ++h) {
+            const int p = h * 32 + lane;
+            float d0, d1;
+            pair_dist2<DP>(tile[0], p, ra2, d0, d1);
+            const int c0 = 2 * p, c1 = 2 * p + 1;
+            v[2 * h] = (row_valid && c0 != r && idx[c0] != kNoIndex) ? make_key(__float_as_uint(d0), idx[c0]) : kKeyMax;
+            v[2 * h + 1] =
+                (row_valid && c1 != r && idx[c1] != kNoIndex) ? make_key(__float_as_uint(d1), idx[c1]) : kKeyMax;
         }
         uint64_t kk = kKeyMax;
         uint64_t best = kKeyMax;  // k <= 32: the 32 best so far, sorted across the warp
@@ -585,9 +594,6 @@ __global__ void __launch_bounds__(kThreads) seed_kernel(const float* __restrict_
             // register across the warp (sorted); keys below the current k-th
             // key gather in shared memory, 32 at most, and join by a bitonic
             // merge in registers
-            float ra[DP];
-#pragma unroll
-            for (int f = 0; f < DP; ++f) ra[f] = tile_coord<DP>(tile[0], r, f);
             int cnt = 0;
             const auto merge_pending = [&]() {
                 uint64_t w[1] = {lane < cnt ? lst[lane] : kKeyMax};
@@ -598,16 +604,13 @@ __global__ void __launch_bounds__(kThreads) seed_kernel(const float* __restrict_
             };
             for (int q = 1; q < qs; ++q) {
                 const unsigned* idq = reinterpret_cast<const unsigned*>(tile[q] + tile_index_off(DP));
+                float dd[4];  // columns 2p and 2p + 1 of pairs p = l and l + 32
+                pair_dist2<DP>(tile[q], lane, ra2, dd[0], dd[1]);
+                pair_dist2<DP>(tile[q], lane + 32, ra2, dd[2], dd[3]);
 #pragma unroll
                 for (int j = 0; j < 4; ++j) {
-                    const int c = j * 32 + lane;
-                    float d2 = 0.0f;  // tile_dist2's arithmetic, row coordinates in registers
-#pragma unroll
-                    for (int f = 0; f < DP; ++f) {
-                        const float t = __fsub_rn(ra[f], tile_coord<DP>(tile[q], c, f));
-                        d2 = __fmaf_rn(t, t, d2);
-                    }
-                    const uint64_t key = idq[c] != kNoIndex ? make_key(__float_as_uint(d2), idq[c]) : kKeyMax;
+                    const int c = 2 * ((j >> 1) * 32 + lane) + (j & 1);
+                    const uint64_t key = idq[c] != kNoIndex ? make_key(__float_as_uint(dd[j]), idq[c]) : kKeyMax;
                     unsigned m = __ballot_sync(0xffffffffu, key < kk);
                     if (m && cnt + __popc(m) > 32) {
                         __syncwarp();
@@ -633,22 +636,16 @@ __global__ void __launch_bounds__(kThreads) seed_kernel(const float* __restrict_
                 const int e = j * 32 + lane;
                 if (e < k) lst[e] = v[j];
             }
-            float ra[DP];
-#pragma unroll
-            for (int f = 0; f < DP; ++f) ra[f] = tile_coord<DP>(tile[0], r, f);
             int cnt = k;
             for (int q = 1; q < qs; ++q) {
                 const unsigned* idq = reinterpret_cast<const unsigned*>(tile[q] + tile_index_off(DP));
+                float dd[4];  // columns 2p and 2p + 1 of pairs p = l and l + 32
+                pair_dist2<DP>(tile[q], lane, ra2, dd[0], dd[1]);
+                pair_dist2<DP>(tile[q], lane + 32, ra2, dd[2], dd[3]);
 #pragma unroll
                 for (int j = 0; j < 4; ++j) {
-                    const int c = j * 32 + lane;
-                    float d2 = 0.0f;  // tile_dist2's arithmetic, row coordinates in registers
-#pragma unroll
-                    for (int f = 0; f < DP; ++f) {
-                        const float t = __fsub_rn(ra[f], tile_coord<DP>(tile[q], c, f));
-                        d2 = __fmaf_rn(t, t, d2);
-                    }
-                    const uint64_t key = idq[c] != kNoIndex ? make_key(__float_as_uint(d2), idq[c]) : kKeyMax;
+                    const int c = 2 * ((j >> 1) * 32 + lane) + (j & 1);
+                    const uint64_t key = idq[c] != kNoIndex ? make_key(__float_as_uint(dd[j]), idq[c]) : kKeyMax;
                     unsigned m = __ballot_sync(0xffffffffu, key < kk);
                     if (m && cnt + __popc(m) > k + 32) {
                         __syncwarp();
