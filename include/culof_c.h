@@ -63,7 +63,10 @@ CULOF_API int culof_device_info(char* buf, size_t cap);
  * The context binds to the device current at creation. */
 CULOF_API int culof_context_create(culof_context** out);
 CULOF_API void culof_context_destroy(culof_context* ctx);
-/* Run on a caller's cudaStream_t (NULL: the context's own stream). */
+/* Run on a caller's cudaStream_t (NULL: the context's own stream). Part of a
+ * call may run on two streams of the context forked from that stream by an
+ * event and joined back to it before the call's later work: everything a
+ * call writes is ordered on the call's stream as if it ran there alone. */
 CULOF_API int culof_context_set_stream(culof_context* ctx, void* cuda_stream);
 CULOF_API int culof_context_synchronize(culof_context* ctx);
 /* CULOF_PATH_* (default AUTO). Every path returns bit-identical results. */

@@ -158,6 +158,32 @@ def test_isolated_rows_do_not_change_lof(ctx, monkeypatch, iso, k):
     np.testing.assert_array_equal(got.view(np.uint32), oracle.lof(X, k).view(np.uint32))
 
 
+def test_results_are_ordered_on_the_callers_stream(ctx):
+    # the small-d path forks its sweep and the isolated rows' pass onto two
+    # internal streams and joins them back: a copy queued on the caller's
+    # stream right after the call (no synchronisation in between) sees the
+    # complete results, call after call
+    torch = torch_cuda()
+    X = synthetic.clusters_with_outliers(30_000, 8, seed=43)
+    n, d, k = X.shape[0], X.shape[1], 20
+    Xc, _, _ = oracle.center(X)
+    o_idx, o_d2, o_kd = oracle.knn(Xc, k)
+    s = torch.cuda.Stream()
+    ctx.set_stream(s.cuda_stream)
+    with torch.cuda.stream(s):
+        dx = torch.from_numpy(X).to("cuda", non_blocking=False)
+        for _ in range(3):
+            idx = torch.full((k, n), -1, dtype=torch.int32, device="cuda")
+            d2 = torch.full((k, n), float("nan"), dtype=torch.float32, device="cuda")
+            kd = torch.full((n,), float("nan"), dtype=torch.float32, device="cuda")
+            ctx.knn_device(dx.data_ptr(), n, d, k, False, idx.data_ptr(), d2.data_ptr(), kd.data_ptr())
+            h_idx, h_d2, h_kd = (t.to("cpu", non_blocking=True) for t in (idx, d2, kd))
+            s.synchronize()
+            np.testing.assert_array_equal(h_idx.numpy(), o_idx)
+            np.testing.assert_array_equal(h_d2.numpy().view(np.uint32), o_d2.view(np.uint32))
+            np.testing.assert_array_equal(h_kd.numpy().view(np.uint32), o_kd.view(np.uint32))
+
+
 def test_auto_selects_the_fast_path_for_small_d(ctx):
     X = synthetic.clusters_with_outliers(6000, 8, seed=1)
     ctx.lof(X, 20)
