@@ -687,34 +687,73 @@ __global__ void __launch_bounds__(kThreads) seed_kernel(const float* __restrict_
 // own (iso_rows_kernel). Their result is the row's split-0 list, so the
 // merge reads it like a sweep result. Which rows move is a performance
 // choice only: every row's k best are exact either way.
-constexpr int kIsoSamples = 512;  // seed k-th keys sampled for the threshold (one per thread)
-constexpr int kIsoTop = 5;        // rows above the 6th largest sample leave (about 1%)
-constexpr int kIsoMaxTiles = 8192;  // the pass keeps 4 gaps of 2 bytes per column tile in shared memory
+constexpr int kIsoBins = 4096;        // histogram of seed k-th distances: their float bits >> 20
+constexpr int kIsoBinShift = 20;
+constexpr int kIsoPerMille = 12;      // about 1.2% of the rows leave
+constexpr int kIsoMaxTiles = 8192;    // the pass keeps 4 gaps of 2 bytes per column tile in shared memory
 
-// One block of kIsoSamples threads: the seed k-th keys of kIsoSamples rows
-// spread evenly over the valid positions [pos0, pos1); the threshold is the
-// (kIsoTop+1)-th largest (each thread counts the samples above its own).
-// Also zeroes the row counter.
-__global__ void __launch_bounds__(kIsoSamples) iso_threshold_kernel(const unsigned long long* __restrict__ kth_shared,
-                                                                     int64_t pos0, int64_t pos1,
-                                                                     unsigned long long* __restrict__ thr,
-                                                                     int* __restrict__ iso_count) {
-    __shared__ __align__(16) uint64_t smp[kIsoSamples];
-    const int i = threadIdx.x;
-    const int64_t len = pos1 - pos0;
-    const uint64_t mine = len > 0 ? kth_shared[pos0 + len * i / kIsoSamples] : kKeyMax;
-    smp[i] = mine;
+// Histogram of the seed k-th distances of the valid positions [pos0, pos1)
+// by the upper 12 bits of their float bits (sign, exponent, 3 mantissa
+// bits: bins one eighth of an octave wide, in increasing order; no k-th key
+// falls in the last bin); per-block counts in shared memory, then one
+// atomic per non-empty bin. hist is zeroed by the caller.
+__global__ void __launch_bounds__(256) iso_hist_kernel(const unsigned long long* __restrict__ kth_shared,
+                                                       int64_t pos0, int64_t pos1, unsigned* __restrict__ hist) {
+    __shared__ unsigned h[kIsoBins];
+    for (int i = threadIdx.x; i < kIsoBins; i += blockDim.x) h[i] = 0;
     __syncthreads();
-    int above = 0, same = 0;
-    const ulonglong2* smp2 = reinterpret_cast<const ulonglong2*>(smp);
-#pragma unroll 8
-    for (int j = 0; j < kIsoSamples / 2; ++j) {
-        const ulonglong2 o = smp2[j];
-        above += (o.x > mine ? 1 : 0) + (o.y > mine ? 1 : 0);
-        same += (o.x == mine ? 1 : 0) + (o.y == mine ? 1 : 0);
+    for (int64_t pos = pos0 + static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; pos < pos1;
+         pos += static_cast<int64_t>(gridDim.x) * blockDim.x)
+        atomicAdd(&h[key_bits(kth_shared[pos]) >> kIsoBinShift], 1u);
+    __syncthreads();
+    for (int i = threadIdx.x; i < kIsoBins; i += blockDim.x)
+        if (h[i]) atomicAdd(&hist[i], h[i]);
+}
+
+// One block: the lowest bin b whose rows and those of every higher bin
+// number at most kIsoPerMille per mille of the valid rows (the highest bins first; at
+// least one row): rows whose seed k-th key lies in bins >= b leave, so the
+// threshold key is the last key below bin b. Also zeroes the row counter.
+__global__ void __launch_bounds__(1024) iso_threshold_kernel(const unsigned* __restrict__ hist, int64_t rows,
+                                                             unsigned long long* __restrict__ thr,
+                                                             int* __restrict__ iso_count) {
+    constexpr int kPer = kIsoBins / 1024;
+    __shared__ unsigned part[1024];
+    const int t = threadIdx.x;
+    // this thread's bins are kPer consecutive ones from the top: bins
+    // [kIsoBins - kPer (t + 1), kIsoBins - kPer t)
+    unsigned own = 0;
+#pragma unroll
+    for (int j = 0; j < kPer; ++j) own += hist[kIsoBins - kPer * (t + 1) + j];
+    part[t] = own;
+    __syncthreads();
+    // inclusive scan from the top (Hillis-Steele over the 1024 partial sums)
+    for (int o = 1; o < 1024; o <<= 1) {
+        const unsigned v = t >= o ? part[t - o] : 0u;
+        __syncthreads();
+        part[t] += v;
+        __syncthreads();
     }
-    if (above <= kIsoTop && above + same > kIsoTop) *thr = mine;  // every such thread holds the same key
-    if (i == 0) *iso_count = 0;
+    const int64_t target = rows * kIsoPerMille / 1000 > 0 ? rows * kIsoPerMille / 1000 : 1;
+    const unsigned above = t > 0 ? part[t - 1] : 0u;  // rows in the bins above this thread's
+    // the thread whose bins take the running count past the target picks
+    // the lowest of its bins that keeps it within the target
+    if (above <= target && part[t] > target) {
+        unsigned run = above;
+        int b = kIsoBins - kPer * t;  // one past this thread's highest bin
+        for (int j = kPer - 1; j >= 0; --j) {
+            const int bin = kIsoBins - kPer * (t + 1) + j;
+            if (run + hist[bin] > target) break;
+            run += hist[bin];
+            b = bin;
+        }
+        *thr = b >= kIsoBins ? ~0ull  // the top bin alone is past the target: no row leaves
+                             : (static_cast<unsigned long long>(static_cast<unsigned>(b) << kIsoBinShift) << 32) - 1ull;
+    }
+    if (t == 0) {
+        if (part[1023] <= target) *thr = 0ull;  // every row (only for a handful of rows)
+        *iso_count = 0;
+    }
 }
 
 // Positions [pos0, pend) of the row tiles: flag[pos] = 1 for the valid rows
@@ -1705,12 +1744,17 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
     // equal k-th keys could otherwise take far more than 1%)
     const int iso_cap = static_cast<int>((pos1 - pos0) / 50 + 32);
     if (small && !tensor && sweep && mt > 0 && pos1 > pos0 && nt <= kIsoMaxTiles && iso_rows_enabled(n)) {
-        char* b = static_cast<char*>(iso_.get(256 + sizeof(int) * static_cast<size_t>(pend - pos0) + padded));
+        char* b = static_cast<char*>(
+            iso_.get(256 + sizeof(int) * static_cast<size_t>(pend - pos0) + padded + 256 + sizeof(unsigned) * kIsoBins));
         unsigned long long* thr = reinterpret_cast<unsigned long long*>(b);
         iso_count = reinterpret_cast<int*>(b + sizeof(unsigned long long));
         iso_list = reinterpret_cast<int*>(b + 256);
         iso_flag = reinterpret_cast<unsigned char*>(iso_list + (pend - pos0));  // indexed by position
-        iso_threshold_kernel<<<1, kIsoSamples, 0, s>>>(kth_shared, pos0, pos1, thr, iso_count);
+        unsigned* hist = reinterpret_cast<unsigned*>(b + 256 + sizeof(int) * static_cast<size_t>(pend - pos0) + padded);
+        CG_CUDA(cudaMemsetAsync(hist, 0, sizeof(unsigned) * kIsoBins, s));
+        iso_hist_kernel<<<grid_for(pos1 - pos0, 256), 256, 0, s>>>(kth_shared, pos0, pos1, hist);
+        CG_LAUNCH_CHECK();
+        iso_threshold_kernel<<<1, 1024, 0, s>>>(hist, pos1 - pos0, thr, iso_count);
         CG_LAUNCH_CHECK();
         iso_mark_kernel<<<grid_for(pend - pos0, 256), 256, 0, s>>>(kth_shared, pos0, pend, n, thr, iso_cap, iso_flag,
                                                                    iso_list, iso_count);
