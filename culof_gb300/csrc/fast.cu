@@ -682,7 +682,7 @@ __global__ void __launch_bounds__(kThreads) seed_kernel(const float* __restrict_
 // its neighbours are far away, so its warp of the sweep can prune almost no
 // column tile) holds its warp busy on nearly every tile while the CTA's
 // other warps skip most of them, and the CTA lasts as long as its busiest
-// warp. About 1% of the rows, those with the largest seed k-th keys, leave
+// warp. About 1.2% of the rows, those with the largest seed k-th keys, leave
 // the sweep (it treats them like padding rows) and take a pass of their
 // own (iso_rows_kernel). Their result is the row's split-0 list, so the
 // merge reads it like a sweep result. Which rows move is a performance
@@ -694,9 +694,10 @@ constexpr int kIsoMaxTiles = 8192;    // the pass keeps 4 gaps of 2 bytes per co
 
 // Histogram of the seed k-th distances of the valid positions [pos0, pos1)
 // by the upper 12 bits of their float bits (sign, exponent, 3 mantissa
-// bits: bins one eighth of an octave wide, in increasing order; no k-th key
-// falls in the last bin); per-block counts in shared memory, then one
-// atomic per non-empty bin. hist is zeroed by the caller.
+// bits: bins one eighth of an octave wide, in increasing order; a row with
+// fewer than k neighbours in its seed window, k-th key kKeyMax, falls in
+// the last bin); per-block counts in shared memory, then one atomic per
+// non-empty bin. hist is zeroed by the caller.
 __global__ void __launch_bounds__(256) iso_hist_kernel(const unsigned long long* __restrict__ kth_shared,
                                                        int64_t pos0, int64_t pos1, unsigned* __restrict__ hist) {
     __shared__ unsigned h[kIsoBins];
