@@ -1452,8 +1452,20 @@ merge_kernel(const uint64_t* __restrict__ seed_keys, const uint64_t* __restrict_
     uint64_t* out = lists + total;
     const int64_t pos = pos0 + static_cast<int64_t>(blockIdx.x) * kMergeWarps + warp;
     if (pos >= pos1) return;
+    // element e of the concatenated lists is key t of list l, e = l k + t
+    // (found by subtraction: e < (S + 1) k, and division by a run-time k is slow)
+    const auto split_index = [k](int e, int& t) {
+        int l = 0;
+        t = e;
+        while (t >= k) {
+            t -= k;
+            ++l;
+        }
+        return l;
+    };
     for (int e = lane; e < total; e += 32) {
-        const int l = e / k, t = e % k;
+        int t;
+        const int l = split_index(e, t);
         lists[e] = (l == 0) ? seed_keys[pos * k + t]
                             : partial[(static_cast<int64_t>(l - 1) * nt * kRT + pos) * k + t];
     }
@@ -1462,8 +1474,8 @@ merge_kernel(const uint64_t* __restrict__ seed_keys, const uint64_t* __restrict_
     for (int e = lane; e < total; e += 32) {
         const uint64_t x = lists[e];
         if (x == kKeyMax) continue;
-        const int l = e / k;
-        int rank = e % k;
+        int rank;
+        const int l = split_index(e, rank);
         for (int o = 0; o < nl && rank < k; ++o) {
             if (o == l) continue;
             const uint64_t* lo = lists + o * k;
