@@ -52,7 +52,7 @@ using namespace sweep;
 
 constexpr int kPairs = kCT / 2;
 constexpr int kRowsPerLane = 4;
-constexpr int kStages = 4;     // column tiles in flight
+constexpr int kStages = 5;     // column tiles in flight
 constexpr int kSeedWindow = 5;  // tiles of the seed: T, T+1, T-1, T+2, T-2
 constexpr int kMaxDP = 8;      // the small-d sweep; wider points take wide.cu's
 constexpr int kMaxWideD = 128;
@@ -1063,11 +1063,16 @@ __global__ void __launch_bounds__(32 * kIsoWarps, 6) iso_rows_kernel(const float
 
 template <int DP, int M>
 struct SweepSmem {
-    float tiles[kStages][tile_floats(DP)];
+    union {
+        float tiles[kStages][tile_floats(DP)];
+        // (-2a, -2a) per row and dimension, the packed FMA operands: every
+        // warp copies its rows into registers before the barrier that
+        // precedes the first tile copy, so they share the tiles' space
+        uint64_t rowd[kRT][DP];
+    };
     RowLists<M> L;
     uint64_t full_bar[kStages];
     float rowc[kRT][DP];
-    uint64_t rowd[kRT][DP];  // (-2a, -2a) per row and dimension: the packed FMA operands
     int done[kStages];
     uint16_t queue[kWarps][kQueueCap];
     float wbox[kWarps][2][DP];  // bounding box of each warp's 16 rows
