@@ -61,8 +61,8 @@ PATH_NAMES = ["auto", "fast", "general", "tensor"]
 # very workload (dram__bytes_read.sum + dram__bytes_write.sum); other
 # workloads report null.
 MEASURED_SWEEP_TRAFFIC = {
-    ("clusters", 200_000, 8, 20): (16_120_000 + 10_320_000,
-                                   "ncu: 16.12 MB read + 10.32 MB written per sweep_kernel launch at this workload "
+    ("clusters", 200_000, 8, 20): (16_110_000 + 10_360_000,
+                                   "ncu: 16.11 MB read + 10.36 MB written per sweep_kernel launch at this workload "
                                    "(the isolated rows' pass beside it: 7.79 MB read)"),
 }
 
