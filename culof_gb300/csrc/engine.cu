@@ -175,12 +175,11 @@ int Engine::choose_path(int64_t n, int d, int k) const {
         throw Error(kInvalidArgument, "fused path requested but unsupported for this n/d/k");
     if (p == kPathFast || p == kPathTensor) return p;
     if (!ok || n <= kSmallN) return kPathGeneral;
-    // d <= 8: the FP32 small-d sweep up to k = 48; above it the tensor sweep
-    // (split f16 operands over the same seed window and prune lists) wins
-    // (fit_predict on clusters, k = 64: n = 20k, 3.3 against 5.4 ms;
-    // n = 200k, 25.5 against 50.1 ms; at k = 48 the FP32 sweep is ahead or
-    // level: 2.3 / 3.2 / 19.0 against 2.4 / 4.8 / 19.1 ms at 20k / 50k / 200k)
-    if (d <= 8) return k > 48 ? kPathTensor : kPathFast;
+    // d <= 8: the FP32 small-d sweep at every k (fit_predict on clusters
+    // against the tensor sweep over the same seed window and prune lists:
+    // k = 64, n = 20k / 50k / 200k: 1.42 / 3.13 / 17.6 against 3.38 / 6.90 /
+    // 25.2 ms; k = 48, 200k: 16.3 against 18.8 ms)
+    if (d <= 8) return kPathFast;
     // 8 < d <= 16 with fewer row tiles than SMs: the FP32 wide sweep ties the
     // tensor path (n = 20k, d = 16: 1.91 against 1.87 ms); from there up the
     // tensor path wins (n = 30k: 2.33 against 2.80 ms; 38k: 3.01 against

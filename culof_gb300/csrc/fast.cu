@@ -1832,16 +1832,17 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
     } else if (nt > 1 && mt > 0 && wide) {
         wide_sweep(tiles, nt, t0, mt, nsplit, d, k, maxn, kth_shared, partial, s);
     } else if (sweep && mt > 0) {
-        // lists of 64 keys for k <= 24, else 96: a list compacts once fewer
-        // than 32 slots are free, so k close to the capacity minus 32 would
-        // compact after every chunk (k = 32 with 64 slots: 1.90 ms against
-        // 1.44 ms for k = 33 with 96, n = 20k)
-        const bool big = k > 24;
-#define CG_SWEEP(DPV)                                                                                              \
-    (big ? launch_sweep<DPV, 96>(tiles, nt, t0, mt, qs, nsplit, k, maxn, kth_shared, partial, status, evaluated, plist, \
-                                 pcount, order, boxes, iso_flag, sweep_s)                                           \
-         : launch_sweep<DPV, 64>(tiles, nt, t0, mt, qs, nsplit, k, maxn, kth_shared, partial, status, evaluated, plist, \
-                                 pcount, order, boxes, iso_flag, sweep_s))
+        // lists of 64 keys for k <= 24, 96 for k <= 48, else 128: a list
+        // compacts once fewer than 32 slots are free, so k close to the
+        // capacity minus 32 would compact after every chunk (k = 32 with 64
+        // slots: 1.90 ms against 1.44 ms for k = 33 with 96, n = 20k; k = 64
+        // with 96 slots: 42.1 ms at n = 200k, against 21.1 ms for k = 56).
+        // Above 64 slots a CTA per SM is what the shared memory allows
+        // anyway.
+#define CG_SWEEP_M(DPV, MV)                                                                                           \
+    launch_sweep<DPV, MV>(tiles, nt, t0, mt, qs, nsplit, k, maxn, kth_shared, partial, status, evaluated, plist, pcount, \
+                          order, boxes, iso_flag, sweep_s)
+#define CG_SWEEP(DPV) (k > 48 ? CG_SWEEP_M(DPV, 128) : k > 24 ? CG_SWEEP_M(DPV, 96) : CG_SWEEP_M(DPV, 64))
         switch (dp) {
             case 2: CG_SWEEP(2); break;
             case 4: CG_SWEEP(4); break;
@@ -1849,6 +1850,7 @@ void Engine::knn_fast(const float* xc, const float* norms, int64_t n, int d, int
             default: CG_SWEEP(8); break;
         }
 #undef CG_SWEEP
+#undef CG_SWEEP_M
     }
     if (iso_flag) {  // the isolated rows' own pass (split-0 lists), on the side stream
         CG_CUDA(cudaEventRecord(high_join_, high_stream_));

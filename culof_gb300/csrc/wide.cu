@@ -351,7 +351,10 @@ void wide_seed(const float* tiles, int nt, int t0, int mt, int d, int k, uint64_
 void wide_sweep(const float* tiles, int nt, int t0, int mt, int nsplit, int d, int k, const unsigned* maxn,
                 unsigned long long* kth_shared, uint64_t* partial, cudaStream_t s) {
     const int dpw = wide_dims_padded(d);
-    if (k > 24) launch_wide_sweep_m<96>(tiles, nt, t0, mt, nsplit, d, dpw, k, maxn, kth_shared, partial, s);
+    // list capacities as the small-d sweep's (k + 32 free slots at least;
+    // with 128 keys the shared memory stays within 218 KB at d = 128)
+    if (k > 48) launch_wide_sweep_m<128>(tiles, nt, t0, mt, nsplit, d, dpw, k, maxn, kth_shared, partial, s);
+    else if (k > 24) launch_wide_sweep_m<96>(tiles, nt, t0, mt, nsplit, d, dpw, k, maxn, kth_shared, partial, s);
     else launch_wide_sweep_m<64>(tiles, nt, t0, mt, nsplit, d, dpw, k, maxn, kth_shared, partial, s);
 }
 

@@ -37,7 +37,7 @@ extern "C" {
 #define CULOF_ERR_KERNEL 5 /* a kernel reported an error status word (e.g. a bounded wait expired) */
 
 /* Path selection for culof_context_set_path. */
-#define CULOF_PATH_AUTO 0    /* GENERAL for n <= 4096; FAST for d <= 8 (k <= 48); TENSOR above; GENERAL past the fused limits */
+#define CULOF_PATH_AUTO 0    /* GENERAL for n <= 4096; FAST for d <= 8; TENSOR above; GENERAL past the fused limits */
 #define CULOF_PATH_FAST 1    /* fused FP32 distance + filtered select (d <= 128, k <= 64) */
 #define CULOF_PATH_GENERAL 2 /* exact distance tile + radix select (any d, any k)        */
 #define CULOF_PATH_TENSOR 3  /* f16 tensor-core filter + exact rescoring (d <= 128, k <= 64) */

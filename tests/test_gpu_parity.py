@@ -131,8 +131,8 @@ ISO_CASES = ["clusters", "clusters_k1", "lowdim", "d5_k25", "ragged", "dups", "k
 @pytest.mark.parametrize("lists", ["1", "0"])
 @pytest.mark.parametrize("name", ISO_CASES)
 def test_knn_with_isolated_rows_bit_exact(ctx, monkeypatch, name, lists):
-    # the rows with the largest seed k-th keys (about 1%) leave the small-d
-    # sweep for their own pass from 65,536 points on; CULOF_ISO_ROWS=1 takes
+    # the rows with the largest seed k-th keys (about 1.2%) leave the small-d
+    # sweep for their own pass from 16,384 points on; CULOF_ISO_ROWS=1 takes
     # that path at any size, with and without the per-tile candidate lists
     monkeypatch.setenv("CULOF_ISO_ROWS", "1")
     monkeypatch.setenv("CULOF_PRUNE_LISTS", lists)
@@ -187,6 +187,10 @@ def test_results_are_ordered_on_the_callers_stream(ctx):
 def test_auto_selects_the_fast_path_for_small_d(ctx):
     X = synthetic.clusters_with_outliers(6000, 8, seed=1)
     ctx.lof(X, 20)
+    assert ctx.last_path() == _culof.PATH_FAST
+    # d <= 8 takes the FP32 sweep at every k the fused paths take (128-key
+    # lists for k > 48)
+    ctx.lof(X, 64)
     assert ctx.last_path() == _culof.PATH_FAST
     # up to 4096 points the general path's few kernels beat the fused paths
     ctx.lof(synthetic.clusters_with_outliers(3000, 8, seed=1), 20)
